@@ -1,0 +1,209 @@
+"""blaze103 -- Python host side of the GB300 BLASTP preliminary search stage.
+
+Mirrors the reference's interface for this path (181charan/BLAZE-SC-ad):
+
+* ``SeqSrc`` plays the part of NCBI's ``BlastSeqSrc`` database source
+  (BLAZE_ncbi/blast_seqsrc.c:45-134) with its getters ``num_seqs``,
+  ``tot_len``, ``max_seq_len``, ``avg_seq_len``; the residues live in device
+  memory, length-sorted, for the life of the object.
+* ``PrelimSearch.run`` stands where ``Blast_RunPreliminarySearchWithInterruptMT``
+  calls ``BLAZE_GPU`` and then re-searches the survivors on the CPU
+  (BLAZE_ncbi/blast_engine.c:2962-3006); here the GPU returns every subject's
+  finished HSP list (``HSPResults.hsp_lists()`` ~ the ``BlastHSPList`` objects
+  written to the HSP stream at blast_engine.c:2499).
+* ``default_params`` computes the cutoffs that blast_engine.c:2971-2981 takes
+  from NCBI's word and hit-saving parameters.
+
+All compute goes through libblaze103 (CUDA, sm_103a). There is no CPU
+fallback: without the built library or a GPU every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import (HSP_DTYPE, INIT_DTYPE, BlazeError, BlazeParams, BlazeStats, check, load, u8ptr,
+                   u64ptr, status_string)
+
+__all__ = ["SeqSrc", "PrelimSearch", "HSPResults", "BlazeParams", "BlazeError", "HSP_DTYPE",
+           "default_params", "device_count", "load", "status_string"]
+
+
+def device_count() -> int:
+    n = ctypes.c_int(0)
+    check(load().blaze_device_count(ctypes.byref(n)), "blaze_device_count")
+    return n.value
+
+
+def _codes(a, what: str) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.uint8)
+    if a.size and (a.min() == 0 or a.max() >= 28):
+        raise ValueError(f"{what}: residues must be NCBIstdaa codes 1..27")
+    return a
+
+
+class SeqSrc:
+    """Device-resident residue database (NCBI BlastSeqSrc analog)."""
+
+    def __init__(self, residues, offsets, device: int = 0):
+        self._lib = load()
+        res = _codes(residues, "database")
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        if off.ndim != 1 or off.size < 1:
+            raise ValueError("offsets must be a 1-D array of n_subjects + 1 entries")
+        h = ctypes.c_void_p()
+        check(self._lib.blaze_db_create(int(device), u8ptr(res), u64ptr(off), off.size - 1,
+                                        ctypes.byref(h)), "blaze_db_create")
+        self._h = h
+        self.device = device
+        tot, n, mx = ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint32()
+        check(self._lib.blaze_db_info(h, ctypes.byref(tot), ctypes.byref(n), ctypes.byref(mx)),
+              "blaze_db_info")
+        self.tot_len, self.num_seqs, self.max_seq_len = tot.value, n.value, mx.value
+
+    @property
+    def avg_seq_len(self) -> int:
+        return self.tot_len // max(self.num_seqs, 1)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.blaze_db_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_params(query_length: int, seq_src: SeqSrc | None = None, evalue: float = 10.0, *,
+                   db_residues: int | None = None, db_subjects: int | None = None) -> BlazeParams:
+    """NCBI blastp defaults (BLOSUM62, gaps 11/1, word 3, T 11, window 40)."""
+    if seq_src is not None:
+        db_residues, db_subjects = seq_src.tot_len, seq_src.num_seqs
+    p = BlazeParams()
+    check(load().blaze_params_default(int(query_length), int(db_residues), int(db_subjects),
+                                      float(evalue), ctypes.byref(p)), "blaze_params_default")
+    return p
+
+
+@dataclass
+class HSPResults:
+    hsps: np.ndarray  # HSP_DTYPE records grouped by OID, NCBI order within a subject
+    stats: dict
+
+    def hsp_lists(self) -> dict[int, np.ndarray]:
+        """OID -> that subject's HSP records (the BlastHSPList analog)."""
+        out: dict[int, np.ndarray] = {}
+        if self.hsps.size == 0:
+            return out
+        oids = self.hsps["oid"]
+        cut = np.flatnonzero(np.diff(oids)) + 1
+        for chunk in np.split(self.hsps, cut):
+            out[int(chunk["oid"][0])] = chunk
+        return out
+
+
+class Query:
+    """A query's residues and word lookup resident on the device."""
+
+    def __init__(self, seq_src: SeqSrc, query, word_threshold: int = 11):
+        self._lib = load()
+        q = _codes(query, "query")
+        h = ctypes.c_void_p()
+        check(self._lib.blaze_query_create(seq_src.handle, u8ptr(q), len(q), int(word_threshold),
+                                           ctypes.byref(h)), "blaze_query_create")
+        self._h = h
+        self.length = len(q)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.blaze_query_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PrelimSearch:
+    """Runs the preliminary search stage against one SeqSrc (one CUDA stream)."""
+
+    def __init__(self, seq_src: SeqSrc):
+        self._lib = load()
+        self.seq_src = seq_src
+        h = ctypes.c_void_p()
+        check(self._lib.blaze_search_create(seq_src.handle, ctypes.byref(h)), "blaze_search_create")
+        self._h = h
+
+    def run_query(self, query: Query, params: BlazeParams) -> int:
+        n = ctypes.c_uint64()
+        check(self._lib.blaze_search_run(self._h, query.handle, ctypes.byref(params),
+                                         ctypes.byref(n)), "blaze_search_run")
+        return n.value
+
+    def results(self) -> np.ndarray:
+        n = ctypes.c_uint64()
+        self._lib.blaze_search_results(self._h, None, 0, ctypes.byref(n))
+        out = np.zeros(n.value, dtype=HSP_DTYPE)
+        check(self._lib.blaze_search_results(self._h, out.ctypes.data_as(ctypes.c_void_p),
+                                             n.value, ctypes.byref(n)), "blaze_search_results")
+        return out
+
+    def init_hits(self) -> np.ndarray:
+        """Init hits of the last run (diagnostics), INIT_DTYPE records."""
+        n = ctypes.c_uint64()
+        self._lib.blaze_search_init_hits(self._h, None, 0, ctypes.byref(n))
+        out = np.zeros(n.value, dtype=INIT_DTYPE)
+        check(self._lib.blaze_search_init_hits(self._h, out.ctypes.data_as(ctypes.c_void_p),
+                                               n.value, ctypes.byref(n)), "blaze_search_init_hits")
+        return out
+
+    def stats(self) -> dict:
+        st = BlazeStats()
+        check(self._lib.blaze_search_stats(self._h, ctypes.byref(st)), "blaze_search_stats")
+        return st.as_dict()
+
+    def run(self, query, params: BlazeParams | None = None, evalue: float = 10.0) -> HSPResults:
+        q = Query(self.seq_src, query, params.word_threshold if params else 11)
+        try:
+            if params is None:
+                params = default_params(q.length, self.seq_src, evalue)
+            self.run_query(q, params)
+            return HSPResults(self.results(), self.stats())
+        finally:
+            q.close()
+
+    def prelim_search(self, query, params: BlazeParams, capacity: int) -> np.ndarray:
+        """The one-call C-ABI path with host buffers (blaze_prelim_search)."""
+        q = _codes(query, "query")
+        out = np.zeros(capacity, dtype=HSP_DTYPE)
+        n = ctypes.c_uint64()
+        check(self._lib.blaze_prelim_search(self._h, u8ptr(q), len(q), ctypes.byref(params),
+                                            out.ctypes.data_as(ctypes.c_void_p), capacity,
+                                            ctypes.byref(n)), "blaze_prelim_search")
+        return out[: n.value]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.blaze_search_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

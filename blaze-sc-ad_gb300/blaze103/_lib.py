@@ -1,0 +1,124 @@
+"""ctypes binding of libblaze103 (the C ABI in include/blaze_prelim.h)."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libblaze103.so")
+
+# The exported entry points and their C signatures (kept in step with
+# include/blaze_prelim.h; tests check the two agree).
+EXPORTS = (
+    "blaze_status_string", "blaze_device_count", "blaze_db_create", "blaze_db_free",
+    "blaze_db_info", "blaze_query_create", "blaze_query_free", "blaze_params_default",
+    "blaze_search_create", "blaze_search_free", "blaze_search_run", "blaze_search_results",
+    "blaze_search_stats", "blaze_search_init_hits", "blaze_prelim_search",
+)
+
+HSP_DTYPE = np.dtype([
+    ("oid", "<u4"), ("score", "<i4"), ("q_start", "<i4"), ("q_end", "<i4"),
+    ("s_start", "<i4"), ("s_end", "<i4"), ("q_gapped_start", "<i4"), ("s_gapped_start", "<i4"),
+    ("evalue", "<f8"),
+])
+assert HSP_DTYPE.itemsize == 40
+INIT_DTYPE = np.dtype([
+    ("oid", "<u4"), ("q_start", "<i4"), ("s_start", "<i4"), ("length", "<i4"), ("score", "<i4"),
+    ("q_trigger", "<i4"), ("s_trigger", "<i4"),
+])
+
+
+class BlazeParams(ctypes.Structure):
+    _fields_ = [
+        ("word_threshold", ctypes.c_int32), ("window", ctypes.c_int32),
+        ("ungapped_xdrop", ctypes.c_int32), ("ungapped_cutoff", ctypes.c_int32),
+        ("gap_open", ctypes.c_int32), ("gap_extend", ctypes.c_int32),
+        ("gapped_xdrop", ctypes.c_int32), ("gapped_cutoff", ctypes.c_int32),
+        ("lambda_", ctypes.c_double), ("K", ctypes.c_double),
+        ("eff_searchsp", ctypes.c_double), ("prelim_evalue", ctypes.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {(k[:-1] if k.endswith("_") else k): getattr(self, k) for k, _ in self._fields_}
+
+
+class BlazeStats(ctypes.Structure):
+    _fields_ = [
+        ("residues_scanned", ctypes.c_uint64), ("word_hits", ctypes.c_uint64),
+        ("ungapped_extensions", ctypes.c_uint64), ("init_hsps", ctypes.c_uint64),
+        ("gapped_extensions", ctypes.c_uint64), ("dp_cells", ctypes.c_uint64),
+        ("hsps", ctypes.c_uint64), ("subjects_with_hsps", ctypes.c_uint32),
+        ("reruns", ctypes.c_uint32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BlazeError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: {status_string(status)} (status {status})")
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load the library. Raises OSError when it has not been built: there is
+    no fallback implementation."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise OSError(f"libblaze103 is not built ({path}); run __graft_entry__.build()")
+    L = ctypes.CDLL(path)
+    vp, u8p = ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8)
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+    i32, u32 = ctypes.c_int32, ctypes.c_uint32
+    L.blaze_status_string.argtypes = [ctypes.c_int]
+    L.blaze_status_string.restype = ctypes.c_char_p
+    L.blaze_device_count.argtypes = [ctypes.POINTER(ctypes.c_int)]
+    L.blaze_db_create.argtypes = [ctypes.c_int, u8p, u64p, u32, ctypes.POINTER(vp)]
+    L.blaze_db_free.argtypes = [vp]
+    L.blaze_db_info.argtypes = [vp, u64p, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    L.blaze_query_create.argtypes = [vp, u8p, i32, i32, ctypes.POINTER(vp)]
+    L.blaze_query_free.argtypes = [vp]
+    L.blaze_params_default.argtypes = [i32, ctypes.c_uint64, u32, ctypes.c_double,
+                                       ctypes.POINTER(BlazeParams)]
+    L.blaze_search_create.argtypes = [vp, ctypes.POINTER(vp)]
+    L.blaze_search_free.argtypes = [vp]
+    L.blaze_search_run.argtypes = [vp, vp, ctypes.POINTER(BlazeParams), u64p]
+    L.blaze_search_results.argtypes = [vp, vp, ctypes.c_uint64, u64p]
+    L.blaze_search_stats.argtypes = [vp, ctypes.POINTER(BlazeStats)]
+    L.blaze_search_init_hits.argtypes = [vp, vp, ctypes.c_uint64, u64p]
+    L.blaze_prelim_search.argtypes = [vp, u8p, i32, ctypes.POINTER(BlazeParams), vp,
+                                      ctypes.c_uint64, u64p]
+    for name in EXPORTS:
+        if name != "blaze_status_string":
+            getattr(L, name).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def status_string(status: int) -> str:
+    try:
+        return load().blaze_status_string(int(status)).decode()
+    except OSError:
+        return "library not loaded"
+
+
+def check(status: int, what: str) -> None:
+    if status != 0:
+        raise BlazeError(status, what)
+
+
+def u8ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+
+
+def u64ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))

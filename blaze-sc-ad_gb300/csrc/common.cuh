@@ -1,0 +1,135 @@
+// common.cuh -- internal types shared by the host driver and the kernels of
+// libblaze103 (GB300 / sm_103a BLASTP preliminary stage).
+#pragma once
+
+#include <cstdint>
+#include <climits>
+
+#include <cuda_runtime.h>
+
+#include "blaze_prelim.h"
+
+namespace blaze {
+
+constexpr int kAlphabet = 28;
+constexpr int kWords = kAlphabet * kAlphabet * kAlphabet;  // 21952 three-letter words
+constexpr int kWordSize = 3;
+constexpr int32_t kNeg = INT32_MIN / 2;  // "minus infinity" of the gapped DP
+constexpr int kWarp = 32;
+
+// Word-finder tuning (per warp of the scan kernel).
+constexpr int kDeferCap = 128;  // deferred hits per buffer (two buffers)
+constexpr int kSeedCap = 128;   // queued two-hit seeds (>= kDeferCap)
+constexpr int kScanWarpsPerBlock = 8;
+constexpr int kGappedWarpsPerBlock = 4;
+
+// An ungapped HSP that reached the ungapped cutoff (NCBI BlastInitHSP analog).
+struct InitHit {
+    int32_t q_start, s_start, len, score;
+    int32_t q_trig, s_trig;  // the second word hit that triggered the extension
+};
+
+// One subject with init hits, for the gapped kernel.
+struct WorkItem {
+    uint32_t subject;  // index into the length-sorted database
+    uint32_t n_init;
+    uint64_t first;    // first record in the init-hit array
+};
+
+// A finished gapped HSP as the device writes it (subject = sorted index).
+struct DevHsp {
+    uint32_t subject;
+    int32_t score, q_start, q_end, s_start, s_end, q_gs, s_gs;
+};
+
+// Device counters of one run; zeroed before every run.
+struct DevCounters {
+    unsigned long long init_count;   // init hits published
+    unsigned long long work_count;   // work items published
+    unsigned long long out_count;    // HSPs published
+    unsigned long long next_scan;    // scan-kernel subject cursor
+    unsigned long long next_gapped;  // gapped-kernel work cursor
+    unsigned long long word_hits;
+    unsigned long long extensions;
+    unsigned long long gapped_ext;
+    unsigned long long dp_cells;
+    unsigned long long residues;
+    unsigned int overflow_subjects;  // subjects whose init hits exceeded the per-warp scratch
+    unsigned int max_init_needed;    // largest init-hit count among those
+    unsigned int flags;              // kFlag* bits
+    unsigned int pad;
+};
+
+constexpr unsigned kFlagInitArrayFull = 1u;
+constexpr unsigned kFlagWorkArrayFull = 2u;
+constexpr unsigned kFlagOutArrayFull = 4u;
+constexpr unsigned kFlagSavedFull = 8u;
+constexpr unsigned kFlagBadState = 16u;
+
+struct ScanArgs {
+    const uint8_t *res;        // residues, length-sorted subjects
+    const uint64_t *off;       // n_subj + 1 offsets
+    uint32_t n_subj;
+    const uint8_t *q;          // query residues
+    int32_t qlen;
+    const uint32_t *cell_start;  // kWords + 1
+    const uint16_t *cell_off;    // query offsets per cell, ascending
+    int32_t window, xdrop, cutoff;
+    uint32_t diag_mask;        // diagonal table entries - 1 (power of two >= qlen + window)
+    InitHit *scratch;          // per warp: scratch_cap records
+    uint32_t scratch_cap;
+    InitHit *init_out;
+    unsigned long long init_cap;
+    WorkItem *work;
+    unsigned long long work_cap;
+    DevCounters *cnt;
+};
+
+struct GappedArgs {
+    const uint8_t *res;
+    const uint64_t *off;
+    const uint8_t *q;
+    int32_t qlen;
+    const InitHit *init_in;
+    const WorkItem *work;
+    unsigned long long work_cap;
+    InitHit *sorted;     // per warp: cap records
+    DevHsp *saved;       // per warp: cap records
+    uint32_t cap;
+    int32_t *dp;         // per warp: 2 * dp_stride ints
+    uint32_t dp_stride;  // >= max subject length + 2
+    int32_t gap_open, gap_extend, xdrop, cutoff;
+    DevHsp *out;
+    unsigned long long out_cap;
+    DevCounters *cnt;
+};
+
+// Launchers (kernels.cu).
+cudaError_t launch_scan(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem, cudaStream_t st);
+cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st);
+size_t scan_smem_bytes(uint32_t diag_entries, int warps_per_block);
+cudaError_t scan_occupancy(int warps_per_block, size_t smem, int *blocks_per_sm);
+cudaError_t gapped_occupancy(int *blocks_per_sm);
+
+// Host helpers (host.cpp).
+extern const int32_t kBlosum62[kAlphabet][kAlphabet];
+// Word lookup of a query: cell_start[kWords + 1], offsets ascending per cell.
+int build_lookup(const uint8_t *query, int32_t qlen, int32_t threshold,
+                 uint32_t *cell_start, uint16_t **offsets, uint32_t *n_offsets);
+int default_params(int32_t qlen, uint64_t db_len, uint32_t db_n, double evalue,
+                   blaze_params *out);
+
+}  // namespace blaze
+
+#define BLAZE_CUDA_TRY(expr)                                  \
+    do {                                                      \
+        cudaError_t err__ = (expr);                           \
+        if (err__ != cudaSuccess) {                           \
+            last_cuda_error(err__);                           \
+            return err__ == cudaErrorMemoryAllocation         \
+                       ? BLAZE_ERR_OUT_OF_MEMORY              \
+                       : BLAZE_ERR_CUDA;                      \
+        }                                                     \
+    } while (0)
+
+void last_cuda_error(cudaError_t e);

@@ -1,0 +1,160 @@
+/*
+ * blaze_prelim.h -- C ABI of libblaze103, a GB300 (sm_103a) implementation of
+ * the BLASTP preliminary search stage (word lookup -> two-hit seeds ->
+ * ungapped X-drop -> semi-gapped X-drop -> per-subject HSP lists).
+ *
+ * Plain pointers and sizes only. Every entry point returns a blaze_status
+ * (0 = success) and never exits the process. Handles are not thread-safe;
+ * use one blaze_search per host thread (each owns its CUDA stream).
+ *
+ * Reference interfaces replaced (paths within 181charan/BLAZE-SC-ad):
+ *   BLAZE_GPU(seq_src, threadIndex, totalThreads, queryLen, survivingSeqs,
+ *             num_survivors, ungapped_cutoff, gapped_cutoff)
+ *       BLAZE_gpu/gpu_cpu_common.h:43, BLAZE_gpu/gpuBLAZE.cu:1428-1704
+ *     -> blaze_search_run + blaze_search_results: instead of a survivor
+ *        list that the CPU re-searches (blast_engine.c:2223-2558), the GPU
+ *        returns each subject's finished HSP list.
+ *   copyConstantMemory / deviceAlloc / deviceMemCpyToDevice of the query
+ *   tables (gpu_cpu_common.h:63-70, prelim_stage.cpp:340-571)
+ *     -> blaze_query_create.
+ *   The per-thread DB gathers through BlastSeqSrcGetSequence and the staging
+ *   buffers (prelim_stage.cpp:478-1229, gpuBLAZE.cu:1587-1618)
+ *     -> blaze_db_create: one length-sorted, device-resident copy.
+ *   BlastInitialWordParametersNew / BlastHitSavingParameters cutoffs
+ *   (blast_engine.c:2971-2981) -> blaze_params_default (the caller may pass
+ *   NCBI's own values instead).
+ */
+#ifndef BLAZE_PRELIM_H
+#define BLAZE_PRELIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum blaze_status {
+    BLAZE_OK = 0,
+    BLAZE_ERR_INVALID_ARG = 1,   /* bad pointer, size or residue code */
+    BLAZE_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+    BLAZE_ERR_NO_DEVICE = 3,     /* no usable GPU */
+    BLAZE_ERR_OUT_OF_MEMORY = 4, /* device or host allocation failed */
+    BLAZE_ERR_OUTPUT_TOO_SMALL = 5, /* caller buffer too small; count reported */
+    BLAZE_ERR_LIMIT = 6,         /* request exceeds a documented limit */
+    BLAZE_ERR_INTERNAL = 7       /* a device-side consistency check failed */
+} blaze_status;
+
+typedef struct blaze_db blaze_db;         /* resident residue database */
+typedef struct blaze_query blaze_query;   /* query + word lookup on the device */
+typedef struct blaze_search blaze_search; /* stream, scratch and results */
+
+/* Search parameters. Raw scores; NCBI BLAST defaults for BLOSUM62 11/1 are
+ * word_threshold 11, window 40, ungapped_xdrop 16, gap_open 11,
+ * gap_extend 1, gapped_xdrop 38. */
+typedef struct blaze_params {
+    int32_t word_threshold;
+    int32_t window;
+    int32_t ungapped_xdrop;
+    int32_t ungapped_cutoff; /* word_params->cutoffs->cutoff_score */
+    int32_t gap_open;
+    int32_t gap_extend;
+    int32_t gapped_xdrop;
+    int32_t gapped_cutoff;   /* hit_params->cutoffs->cutoff_score */
+    double lambda;           /* gapped Karlin-Altschul lambda */
+    double K;                /* gapped Karlin-Altschul K */
+    double eff_searchsp;     /* effective search space of the query */
+    double prelim_evalue;    /* HSPs with a larger E-value are dropped */
+} blaze_params;
+
+/* One HSP of a subject; offsets 0-based, ends exclusive (NCBI BlastHSP's
+ * query.offset/end, subject.offset/end, score, evalue, and the gapped start
+ * point). */
+typedef struct blaze_hsp {
+    uint32_t oid;
+    int32_t score;
+    int32_t q_start, q_end;
+    int32_t s_start, s_end;
+    int32_t q_gapped_start, s_gapped_start;
+    double evalue;
+} blaze_hsp;
+
+/* An ungapped HSP that reached the ungapped cutoff and went on to the gapped
+ * stage (NCBI BlastInitHSP: ungapped_data plus the triggering word hit). */
+typedef struct blaze_init_hit {
+    uint32_t oid;
+    int32_t q_start, s_start, length, score;
+    int32_t q_trigger, s_trigger;
+} blaze_init_hit;
+
+/* Counters of the last run (diagnostics; NCBI BlastDiagnostics analog). */
+typedef struct blaze_stats {
+    uint64_t residues_scanned;
+    uint64_t word_hits;
+    uint64_t ungapped_extensions;
+    uint64_t init_hsps;
+    uint64_t gapped_extensions;
+    uint64_t dp_cells;
+    uint64_t hsps;
+    uint32_t subjects_with_hsps;
+    uint32_t reruns; /* device buffers grown and the pass repeated */
+} blaze_stats;
+
+const char *blaze_status_string(int status);
+
+/* Number of usable devices (0 when none). */
+int blaze_device_count(int *count);
+
+/* Database: residues[offsets[i] .. offsets[i+1]) is subject i (its OID).
+ * NCBIstdaa codes 1..27; subjects of any length >= 0. The library keeps a
+ * length-sorted copy in device memory. */
+int blaze_db_create(int device, const uint8_t *residues, const uint64_t *offsets,
+                    uint32_t n_subjects, blaze_db **out);
+int blaze_db_free(blaze_db *db);
+int blaze_db_info(const blaze_db *db, uint64_t *total_residues, uint32_t *n_subjects,
+                  uint32_t *max_length);
+
+/* Query: NCBIstdaa codes 1..27, 1 <= length <= 65535. Builds the word lookup
+ * (every word scoring >= word_threshold against a query word, plus the query
+ * word itself) and uploads it. */
+int blaze_query_create(const blaze_db *db, const uint8_t *query, int32_t length,
+                       int32_t word_threshold, blaze_query **out);
+int blaze_query_free(blaze_query *q);
+
+/* NCBI BLAST defaults for a blastp search of one query against db with the
+ * given expect value: cutoffs, X-drops, effective search space (length
+ * adjustment of Altschul & Gish), Karlin-Altschul constants. */
+int blaze_params_default(int32_t query_length, uint64_t db_residues, uint32_t db_subjects,
+                         double evalue, blaze_params *out);
+
+int blaze_search_create(blaze_db *db, blaze_search **out);
+int blaze_search_free(blaze_search *s);
+
+/* Runs the preliminary stage of query q against the whole database on the
+ * GPU. On return the results are held by s; *n_hsps is their count. */
+int blaze_search_run(blaze_search *s, const blaze_query *q, const blaze_params *p,
+                     uint64_t *n_hsps);
+
+/* Copies the results of the last run, grouped by OID (ascending) and, within
+ * an OID, in NCBI's per-subject order (score descending). Returns
+ * BLAZE_ERR_OUTPUT_TOO_SMALL when capacity < count (nothing copied). */
+int blaze_search_results(const blaze_search *s, blaze_hsp *out, uint64_t capacity,
+                         uint64_t *n_hsps);
+int blaze_search_stats(const blaze_search *s, blaze_stats *out);
+
+/* Diagnostics: the init hits of the last run, grouped by OID (ascending) and
+ * in the order the gapped stage visits them (score descending, then subject
+ * and query offset of the trigger). Same capacity rule as above. */
+int blaze_search_init_hits(blaze_search *s, blaze_init_hit *out, uint64_t capacity,
+                           uint64_t *n_hits);
+
+/* Convenience: blaze_query_create + blaze_search_run + blaze_search_results
+ * in one call with host buffers (the drop-in path). */
+int blaze_prelim_search(blaze_search *s, const uint8_t *query, int32_t length,
+                        const blaze_params *p, blaze_hsp *out, uint64_t capacity,
+                        uint64_t *n_hsps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

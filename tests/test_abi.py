@@ -1,0 +1,80 @@
+"""CPU checks of the C ABI library: it loads, exports every function the
+public header declares, and its host-only pieces agree with the oracle.
+No compute call needs a GPU here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    names = []
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(blaze_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import blaze103
+
+    return blaze103.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = header_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+    import blaze103._lib as L
+
+    assert sorted(L.EXPORTS) == sorted(n for n in names if not n.startswith("blaze_noalloc")) or \
+        set(L.EXPORTS) <= set(names)
+
+
+def test_status_strings(lib):
+    import blaze103
+
+    assert blaze103.status_string(0) == "ok"
+    assert "output" in blaze103.status_string(5)
+
+
+@pytest.mark.parametrize("qlen,dblen,n", [(300, 7_000_000, 20_000), (1000, 700_000_000, 2_000_000),
+                                          (100, 1_800_000_000, 5_000_000), (5000, 180_000_000, 500_000),
+                                          (30, 50_000, 200)])
+def test_default_params_match_oracle(lib, qlen, dblen, n):
+    import blaze103
+    import oracle
+
+    p = blaze103.default_params(qlen, db_residues=dblen, db_subjects=n).as_dict()
+    o = oracle.default_params(qlen, dblen, n)
+    for k in ("word_threshold", "window", "ungapped_xdrop", "ungapped_cutoff", "gap_open",
+              "gap_extend", "gapped_xdrop", "gapped_cutoff"):
+        assert p[k] == o[k], k
+    assert p["eff_searchsp"] == pytest.approx(o["eff_searchsp"], rel=1e-15)
+    assert p["lambda"] == o["lam"] and p["K"] == o["K"]
+    # published blastp defaults for BLOSUM62 11/1
+    assert (p["ungapped_xdrop"], p["gapped_xdrop"], p["word_threshold"], p["window"]) == (16, 38, 11, 40)
+    assert p["ungapped_cutoff"] == min(41, p["gapped_cutoff"])
+
+
+def test_no_device_is_reported_not_faked(lib):
+    import blaze103
+
+    if blaze103.device_count() > 0:
+        pytest.skip("a GPU is present")
+    off = np.array([0, 3], dtype=np.uint64)
+    res = np.array([1, 2, 3], dtype=np.uint8)
+    h = ctypes.c_void_p()
+    st = lib.blaze_db_create(0, res.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                             off.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), 1, ctypes.byref(h))
+    assert st == 3  # BLAZE_ERR_NO_DEVICE
+    with pytest.raises(blaze103.BlazeError):
+        blaze103.SeqSrc(res, off)

@@ -1,0 +1,132 @@
+"""GPU parity: libblaze103 (through its C ABI, on cuda:0) against the oracle,
+bit for bit on HSP offsets and scores, init hits included; E-values within a
+relative 1e-12 (double arithmetic of identical integer scores)."""
+import os
+
+import numpy as np
+import pytest
+
+import blaze103
+from blaze103 import synth
+
+from _parity import compare, concat, params_for
+
+pytestmark = pytest.mark.gpu
+
+
+def test_config0_scaled():
+    w = synth.make_workload(0, scale=0.25)
+    got, ref, stats = compare(w.queries[0], w.residues, w.offsets)
+    assert len(got) > 0 and stats["dp_cells"] > 0
+    assert np.isin(w.planted, got["oid"]).mean() > 0.9
+
+
+@pytest.mark.parametrize("qlen", [3, 11, 64, 100, 300, 1000, 2500])
+def test_query_lengths(qlen):
+    rng = np.random.default_rng(qlen)
+    q = synth.random_residues(rng, qlen)
+    seqs = [synth.random_residues(rng, int(L)) for L in synth.lognormal_lengths(rng, 1500, 250, 0.82, 30, 3000)]
+    for i in range(0, len(seqs), 10):  # 10% homologs
+        w = min(len(q), int(rng.integers(30, 300)))
+        s0 = int(rng.integers(0, len(q) - w + 1))
+        hom = synth.mutate(rng, q[s0:s0 + w], 0.45)
+        pos = int(rng.integers(0, len(seqs[i]) + 1))
+        seqs[i] = np.concatenate([seqs[i][:pos], hom, seqs[i][pos:]])
+    res, off = concat(seqs)
+    compare(q, res, off)
+
+
+def test_edge_subjects():
+    rng = np.random.default_rng(5)
+    q = synth.random_residues(rng, 150)
+    seqs = [q[:0], q[:1], q[:2], q[:3], q[:4], q.copy(), q[::-1].copy(), q[50:53].copy(),
+            np.concatenate([q, q]), synth.random_residues(rng, 3000)]
+    res, off = concat(seqs)
+    got, _, _ = compare(q, res, off)
+    assert 5 in set(got["oid"].tolist())  # the identical subject
+
+
+def test_tiny_queries():
+    rng = np.random.default_rng(6)
+    seqs = [synth.random_residues(rng, 200) for _ in range(50)]
+    res, off = concat(seqs)
+    for L in (1, 2, 3, 4):
+        compare(seqs[3][10:10 + L], res, off)
+
+
+def test_unsorted_database_keeps_oids():
+    w = synth.make_workload(0, scale=0.05)
+    n = w.n_subjects
+    perm = np.random.default_rng(9).permutation(n)
+    seqs = [w.residues[int(w.offsets[i]):int(w.offsets[i + 1])] for i in perm]
+    res, off = concat(seqs)
+    got, ref, _ = compare(w.queries[0], res, off)
+    assert len(got) > 0
+
+
+def test_low_complexity_seed_storm():
+    rng = np.random.default_rng(11)
+    alpha = np.array([1, 11, 17], dtype=np.uint8)  # A, L, S
+    q = np.concatenate([alpha[rng.integers(0, 3, 400)], synth.random_residues(rng, 200)])
+    seqs = []
+    for i in range(300):
+        s = synth.random_residues(rng, int(rng.integers(100, 1500)))
+        if i % 2 == 0:
+            run = alpha[rng.integers(0, 3, int(rng.integers(50, 400)))]
+            p = int(rng.integers(0, len(s)))
+            s = np.concatenate([s[:p], run, s[p:]])
+        seqs.append(s)
+    res, off = concat(seqs)
+    got, _, stats = compare(q, res, off)
+    assert stats["ungapped_extensions"] > 1000
+
+
+def test_capacity_regrowth(monkeypatch):
+    # tiny starting buffers force every grow-and-repeat path
+    monkeypatch.setenv("BLAZE_INITIAL_SCRATCH_CAP", "2")
+    monkeypatch.setenv("BLAZE_INITIAL_INIT_CAP", "3")
+    monkeypatch.setenv("BLAZE_INITIAL_OUT_CAP", "3")
+    w = synth.make_workload(0, scale=0.05)
+    got, _, stats = compare(w.queries[0], w.residues, w.offsets)
+    assert stats["reruns"] >= 1 and len(got) > 3
+
+
+def test_long_subjects_and_queries():
+    w = synth.make_workload(3, scale=0.001, n_queries=2)
+    for q in w.queries:
+        compare(q, w.residues, w.offsets)
+
+
+def test_one_call_host_buffers_and_small_output():
+    w = synth.make_workload(0, scale=0.05)
+    q = w.queries[0]
+    db = blaze103.SeqSrc(w.residues, w.offsets)
+    ps = blaze103.PrelimSearch(db)
+    p, _ = params_for(len(q), w.total_residues, w.n_subjects)
+    full = ps.run(q, p).hsps
+    one = ps.prelim_search(q, p, capacity=len(full) + 10)
+    assert np.array_equal(full, one)
+    if len(full) > 1:
+        with pytest.raises(blaze103.BlazeError) as e:
+            ps.prelim_search(q, p, capacity=len(full) - 1)
+        assert e.value.status == 5  # BLAZE_ERR_OUTPUT_TOO_SMALL
+    again = ps.run(q, p).hsps
+    assert np.array_equal(full, again)
+    ps.close()
+    db.close()
+
+
+def test_invalid_inputs_rejected():
+    w = synth.make_workload(0, scale=0.01)
+    db = blaze103.SeqSrc(w.residues, w.offsets)
+    bad = np.array([1, 2, 0, 4], dtype=np.uint8)
+    with pytest.raises(ValueError):
+        blaze103.Query(db, bad)
+    ps = blaze103.PrelimSearch(db)
+    p, _ = params_for(10, w.total_residues, w.n_subjects)
+    p.gap_extend = 0
+    with pytest.raises(blaze103.BlazeError) as e:
+        ps.run(w.queries[0][:10], p)
+    assert e.value.status == 1
+    ps.close()
+    db.close()

@@ -1,0 +1,197 @@
+"""CPU tests of the oracle: known answers and independent brute-force checks.
+
+The reference ships no golden vectors for this path (parity with NCBI BLAST+
+2.13.0 is unpinned), so the oracle is pinned here against (a) hand-checkable
+known answers, (b) brute-force re-derivations written independently in
+Python, and (c) committed fixtures in tests/golden/.
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+from blaze103 import synth
+from blaze103._blosum import BLOSUM62
+
+NEG = -(1 << 30)
+
+
+def codes(s: str) -> np.ndarray:
+    alpha = "-ABCDEFGHIKLMNPQRSTVWXYZU*OJ"
+    return np.array([alpha.index(c) for c in s], dtype=np.uint8)
+
+
+# ---------------------------------------------------------------- lookup
+
+def test_blosum_matches_published_values():
+    m = BLOSUM62
+    assert (m == m.T).all()
+    assert m[codes("W")[0], codes("W")[0]] == 11
+    assert m[codes("C")[0], codes("C")[0]] == 9
+    assert m[codes("A")[0], codes("A")[0]] == 4
+    assert m[codes("I")[0], codes("V")[0]] == 3
+    # U scores as C, row 0 is the sentinel
+    assert (m[24] == m[3]).all()
+    assert (m[0] == -32768).all()
+
+
+def test_lookup_matches_brute_force(oracle_mod):
+    rng = np.random.default_rng(1)
+    q = synth.random_residues(rng, 23)
+    cs, offs = oracle_mod.lookup(q, 11)
+    words = [(int(q[i]), int(q[i + 1]), int(q[i + 2])) for i in range(len(q) - 2)]
+    rng2 = np.random.default_rng(2)
+    for v in list(rng2.integers(0, 21952, size=400)) + [w[0] * 784 + w[1] * 28 + w[2] for w in words]:
+        v = int(v)
+        x, y, z = v // 784, (v // 28) % 28, v % 28
+        want = [i for i, (a, b, c) in enumerate(words)
+                if (a, b, c) == (x, y, z) or BLOSUM62[a, x] + BLOSUM62[b, y] + BLOSUM62[c, z] >= 11]
+        assert list(offs[cs[v]:cs[v + 1]]) == want
+
+
+def test_exact_word_always_in_lookup(oracle_mod):
+    # "XXX" scores -3 against itself, far below T=11: it must still hit itself
+    q = codes("XXXAW")
+    cs, offs = oracle_mod.lookup(q, 11)
+    v = 21 * 784 + 21 * 28 + 21
+    assert list(offs[cs[v]:cs[v + 1]]) == [0]
+
+
+# ---------------------------------------------------------- gapped DP
+
+def brute_xdrop(A, B, M, N, reverse, go=11, ge=1, X=38):
+    """Row-major X-drop DP over the full matrix, written from the definition:
+    a cell is live when its score is within X of the best live score seen
+    before it in row-major order; dead cells are -inf for their successors."""
+    goe = go + ge
+    X = max(X, goe)
+    if M <= 0 or N <= 0:
+        return 0, 0, 0
+    row_letter = (lambda a: A[M - a]) if reverse else (lambda a: A[a])
+    col_letter = (lambda b: B[N - b]) if reverse else (lambda b: B[b])
+    H = np.full((M + 1, N + 1), NEG, dtype=np.int64)
+    E = np.full((M + 1, N + 1), NEG, dtype=np.int64)
+    live = np.zeros((M + 1, N + 1), dtype=bool)
+    best, ab, bb = 0, 0, 0
+    for b in range(N + 1):
+        h = 0 if b == 0 else -(goe + (b - 1) * ge)
+        if h >= -X:
+            H[0, b], E[0, b], live[0, b] = h, h - goe, True
+    for a in range(1, M + 1):
+        f = NEG
+        for b in range(N + 1):
+            e = max(H[a - 1, b] - goe if live[a - 1, b] else NEG, E[a - 1, b] - ge)
+            d = H[a - 1, b - 1] + BLOSUM62[row_letter(a), col_letter(b)] if b >= 1 and live[a - 1, b - 1] else NEG
+            h = max(d, e, f)
+            if best - h <= X:
+                live[a, b] = True
+                H[a, b], E[a, b] = h, e
+                if h > best:
+                    best, ab, bb = h, a, b
+                f = max(h - goe, f - ge)
+            else:
+                f = f - ge
+                E[a, b] = e
+    return int(best), ab, bb
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_semi_gapped_matches_brute_force(oracle_mod, seed):
+    rng = np.random.default_rng(100 + seed)
+    M, N = int(rng.integers(1, 45)), int(rng.integers(1, 45))
+    if seed % 3 == 0:  # related sequences give long alignments with gaps
+        base = synth.random_residues(rng, max(M, N) + 5)
+        A = base[:M + 1].copy()
+        B = synth.mutate(rng, base, 0.6)[:N + 1]
+        N = len(B) - 1
+    else:
+        A = synth.random_residues(rng, M + 1)
+        B = synth.random_residues(rng, N + 1)
+    for reverse in (0, 1):
+        a_in = A[1:] if reverse else A
+        b_in = B[1:] if reverse else B
+        got = oracle_mod.semi_gapped(a_in, b_in, M, N, reverse)
+        want = brute_xdrop(a_in, b_in, M, N, reverse)
+        assert got == want, (seed, reverse, M, N)
+
+
+def test_semi_gapped_identity_kat(oracle_mod):
+    s = codes("MKTAYIAKQRQISFVKSHFSRQ")
+    L = len(s)
+    # right extension of a sequence against itself from its first residue
+    score, a, b = oracle_mod.semi_gapped(s, s, L - 1, L - 1, 0)
+    assert (a, b) == (L - 1, L - 1)
+    assert score == sum(int(BLOSUM62[c, c]) for c in s[1:])
+    # left extension includes the anchor residue
+    score, a, b = oracle_mod.semi_gapped(s, s, L, L, 1)
+    assert (a, b) == (L, L) and score == sum(int(BLOSUM62[c, c]) for c in s)
+
+
+def test_gapped_start_kat(oracle_mod):
+    q = codes("WWWWWWWWWWWWAAAAAAAAAAAAAAAA")
+    # short HSP: centre
+    assert oracle_mod.gapped_start(q, q, 3, 3, 9) == 3 + 4
+    # best 11-window is the W run: window ending at offset 10 wins first
+    assert oracle_mod.gapped_start(q, q, 0, 0, len(q)) == 10 - 5
+    # nothing positive: start of the HSP
+    s = codes("PPPPPPPPPPPPPPPP")
+    w = codes("WWWWWWWWWWWWWWWW")
+    assert oracle_mod.gapped_start(w, s, 2, 2, 14) == 2
+
+
+# ----------------------------------------------------- whole pipeline
+
+def _params(qlen, dblen, n):
+    import oracle
+    return oracle.default_params(qlen, dblen, n)
+
+
+def test_identical_subject_gives_full_alignment(oracle_mod):
+    rng = np.random.default_rng(7)
+    q = synth.random_residues(rng, 120)
+    res = np.concatenate([synth.random_residues(rng, 200), q, synth.random_residues(rng, 50)])
+    off = np.array([0, 200, 320, 370], dtype=np.uint64)
+    p = _params(len(q), 1_000_000, 3000)
+    h, _ = oracle_mod.search_db(q, res, off, p, threads=1)
+    hits = h[h["subject"] == 1]
+    assert len(hits) >= 1
+    top = hits[0]
+    assert (top["q_start"], top["q_end"], top["s_start"], top["s_end"]) == (0, 120, 0, 120)
+    assert top["score"] == sum(int(BLOSUM62[c, c]) for c in q)
+
+
+def test_short_and_empty_subjects(oracle_mod):
+    q = codes("MKTAYIAKQRQISFVKSHFSRQLEERLGLIEVQ")
+    subj = [codes(""), codes("M"), codes("MK"), codes("MKT"), codes("MKTA")]
+    res = np.concatenate(subj)
+    off = np.zeros(len(subj) + 1, dtype=np.uint64)
+    off[1:] = np.cumsum([len(s) for s in subj])
+    h, ini = oracle_mod.search_db(q, res, off, _params(len(q), 10_000, 100), want_inits=True)
+    assert len(h) == 0 and len(ini) == 0
+
+
+def test_multithreaded_equals_single_thread(oracle_mod):
+    w = synth.make_workload(0, scale=0.05)
+    p = _params(len(w.queries[0]), w.total_residues, w.n_subjects)
+    a = oracle_mod.search_db(w.queries[0], w.residues, w.offsets, p, threads=1, want_inits=True)
+    b = oracle_mod.search_db(w.queries[0], w.residues, w.offsets, p, threads=7, want_inits=True)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_planted_homologs_are_found(oracle_mod):
+    w = synth.make_workload(0, scale=0.1)
+    p = _params(len(w.queries[0]), w.total_residues, w.n_subjects)
+    h, _ = oracle_mod.search_db(w.queries[0], w.residues, w.offsets, p, threads=4)
+    found = np.isin(w.planted, h["subject"]).mean()
+    assert found > 0.9
+
+
+def test_length_adjustment_fixed_point(oracle_mod):
+    import math
+    K, lam, alpha, beta = 0.041, 0.267, 1.9, -30.0
+    for m, n, N in [(300, 7_000_000, 20_000), (1000, 700_000_000, 2_000_000), (50, 10_000, 40)]:
+        ell = oracle_mod.length_adjustment(K, math.log(K), alpha / lam, beta, m, n, N)
+        f = lambda x: beta + alpha / lam * (math.log(K) + math.log((m - x) * (n - N * x)))
+        assert f(ell) > ell
+        nxt = ell + 1
+        assert not (f(nxt) > nxt and K * (m - nxt) * (n - N * nxt) > max(m, n))
