@@ -50,7 +50,9 @@ class BlazeStats(ctypes.Structure):
         ("ungapped_extensions", ctypes.c_uint64), ("init_hsps", ctypes.c_uint64),
         ("gapped_extensions", ctypes.c_uint64), ("dp_cells", ctypes.c_uint64),
         ("hsps", ctypes.c_uint64), ("subjects_with_hsps", ctypes.c_uint32),
-        ("reruns", ctypes.c_uint32),
+        ("reruns", ctypes.c_uint32), ("scan_ms", ctypes.c_float), ("gapped_ms", ctypes.c_float),
+        ("device_ms", ctypes.c_float), ("kernel_launches", ctypes.c_uint32),
+        ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
     ]
 
     def as_dict(self) -> dict:

@@ -61,15 +61,17 @@ def _substitution_tables() -> np.ndarray:
     return cdf
 
 
+_CDF = _substitution_tables()
+
+
 def mutate(rng: np.random.Generator, seq: np.ndarray, identity: float, indel_rate: float = 0.02,
            indel_mean: float = 3.0) -> np.ndarray:
     seq = np.array(seq, dtype=np.uint8)
-    cdf = _substitution_tables()
-    sub = rng.random(len(seq)) >= identity
-    u = rng.random(len(seq))
-    for i in np.flatnonzero(sub):
-        j = int(np.searchsorted(cdf[seq[i]], u[i], side="right"))
-        seq[i] = STD_CODES[min(j, len(STD_CODES) - 1)]
+    cdf = _CDF
+    sub = np.flatnonzero(rng.random(len(seq)) >= identity)
+    u = rng.random(len(sub))
+    j = (cdf[seq[sub]] <= u[:, None]).sum(axis=1)
+    seq[sub] = STD_CODES[np.minimum(j, len(STD_CODES) - 1)]
     out = []
     i = 0
     events = np.flatnonzero(rng.random(len(seq)) < indel_rate)

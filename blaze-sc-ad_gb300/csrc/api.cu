@@ -36,6 +36,7 @@ struct blaze_query {
     int device = 0;
     int32_t qlen = 0;
     int32_t threshold = 0;
+    uint64_t upload_bytes = 0;  // host->device bytes of the tables
     uint8_t *d_q = nullptr;
     uint32_t *d_cell_start = nullptr;
     uint16_t *d_cell_off = nullptr;
@@ -81,6 +82,7 @@ struct blaze_search {
     std::vector<blaze_hsp> results;
     blaze_stats stats{};
     unsigned long long last_init_count = 0, last_work_count = 0;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 static bool valid_residues(const uint8_t *r, uint64_t n) {
@@ -209,6 +211,7 @@ extern "C" int blaze_query_create(const blaze_db *db, const uint8_t *query, int3
     if (e == cudaSuccess) e = cudaMemcpy(q->d_cell_start, cs.data(), sizeof(uint32_t) * (kWords + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n_off) e = cudaMemcpy(q->d_cell_off, offs, sizeof(uint16_t) * n_off, cudaMemcpyHostToDevice);
     std::free(offs);
+    q->upload_bytes = static_cast<uint64_t>(length) + sizeof(uint32_t) * (kWords + 1) + sizeof(uint16_t) * n_off;
     if (e != cudaSuccess) {
         last_cuda_error(e);
         blaze_query_free(q);
@@ -238,6 +241,7 @@ extern "C" int blaze_search_create(blaze_db *db, blaze_search **out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_cnt, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_cnt, sizeof(DevCounters));
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&s->ev[i]);
     int per_sm = 0;
     if (e == cudaSuccess) e = gapped_occupancy(&per_sm);
     if (e != cudaSuccess) {
@@ -271,6 +275,8 @@ extern "C" int blaze_search_free(blaze_search *s) {
     if (s->d_cnt) cudaFree(s->d_cnt);
     if (s->h_cnt) cudaFreeHost(s->h_cnt);
     if (s->h_out) cudaFreeHost(s->h_out);
+    for (cudaEvent_t ev : s->ev)
+        if (ev) cudaEventDestroy(ev);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return BLAZE_OK;
@@ -301,6 +307,7 @@ static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p
     if ((rc = s->dp.ensure(gapped_warps * 2 * dp_stride)) != BLAZE_OK) return rc;
 
     BLAZE_CUDA_TRY(cudaMemsetAsync(s->d_cnt, 0, sizeof(DevCounters), s->stream));
+    BLAZE_CUDA_TRY(cudaEventRecord(s->ev[1], s->stream));
     ScanArgs sa{};
     sa.res = db->d_res;
     sa.off = db->d_off;
@@ -321,6 +328,7 @@ static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p
     sa.work_cap = s->work.n;
     sa.cnt = s->d_cnt;
     BLAZE_CUDA_TRY(launch_scan(sa, scan_blocks, warps_per_block, smem, s->stream));
+    BLAZE_CUDA_TRY(cudaEventRecord(s->ev[2], s->stream));
 
     GappedArgs ga{};
     ga.res = db->d_res;
@@ -343,6 +351,9 @@ static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p
     ga.out_cap = s->out_cap;
     ga.cnt = s->d_cnt;
     BLAZE_CUDA_TRY(launch_gapped(ga, s->gapped_blocks, s->stream));
+    BLAZE_CUDA_TRY(cudaEventRecord(s->ev[3], s->stream));
+    s->stats.kernel_launches += 2;
+    s->stats.d2h_bytes += sizeof(DevCounters);
     BLAZE_CUDA_TRY(cudaMemcpyAsync(s->h_cnt, s->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, s->stream));
     BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
     return BLAZE_OK;
@@ -357,6 +368,7 @@ extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const bla
     BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
     s->results.clear();
     s->stats = blaze_stats{};
+    s->stats.h2d_bytes = q->upload_bytes;
     if (n_hsps) *n_hsps = 0;
 
     uint32_t entries = 1;
@@ -371,9 +383,15 @@ extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const bla
     const int scan_blocks = s->n_sm * std::max(per_sm, 1);
 
     DevCounters c{};
+    BLAZE_CUDA_TRY(cudaEventRecord(s->ev[0], s->stream));
     for (int attempt = 0;; ++attempt) {
         if ((rc = run_pass(s, q, p, entries, wpb, scan_blocks, smem)) != BLAZE_OK) return rc;
         c = *s->h_cnt;
+        {
+            float ms = 0.f;
+            BLAZE_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev[2], s->ev[3]));
+            s->stats.gapped_ms = ms;
+        }
         if (c.flags & kFlagBadState) return BLAZE_ERR_INTERNAL;
         bool again = false;
         if (c.overflow_subjects > 0) {
@@ -405,7 +423,16 @@ extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const bla
     }
     if (n_out) {
         BLAZE_CUDA_TRY(cudaMemcpyAsync(s->h_out, s->out.p, sizeof(DevHsp) * n_out, cudaMemcpyDeviceToHost, s->stream));
-        BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        s->stats.d2h_bytes += sizeof(DevHsp) * n_out;
+    }
+    BLAZE_CUDA_TRY(cudaEventRecord(s->ev[3], s->stream));
+    BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    {
+        float ms = 0.f;
+        BLAZE_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev[1], s->ev[2]));
+        s->stats.scan_ms = ms;
+        BLAZE_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev[0], s->ev[3]));
+        s->stats.device_ms = ms;
     }
     // groups: each subject's HSPs are contiguous and already in final order
     struct Group { uint32_t oid; size_t first, n; };

@@ -98,6 +98,13 @@ typedef struct blaze_stats {
     uint64_t hsps;
     uint32_t subjects_with_hsps;
     uint32_t reruns; /* device buffers grown and the pass repeated */
+    /* CUDA-event times on the search stream, last pass only (milliseconds) */
+    float scan_ms;   /* word finder + ungapped kernel */
+    float gapped_ms; /* gapped kernel */
+    float device_ms; /* first to last device operation of the run, all passes */
+    uint32_t kernel_launches; /* kernels launched by the run, all passes */
+    uint64_t h2d_bytes; /* host->device bytes of the run (query tables included) */
+    uint64_t d2h_bytes; /* device->host bytes of the run */
 } blaze_stats;
 
 const char *blaze_status_string(int status);
@@ -114,7 +121,7 @@ int blaze_db_free(blaze_db *db);
 int blaze_db_info(const blaze_db *db, uint64_t *total_residues, uint32_t *n_subjects,
                   uint32_t *max_length);
 
-/* Query: NCBIstdaa codes 1..27, 1 <= length <= 65535. Builds the word lookup
+/* Query: NCBIstdaa codes 1..27, 1 <= length <= 32000. Builds the word lookup
  * (every word scoring >= word_threshold against a query word, plus the query
  * word itself) and uploads it. */
 int blaze_query_create(const blaze_db *db, const uint8_t *query, int32_t length,

@@ -67,32 +67,68 @@ static int word_is_neighbour(int w, int v, int32_t threshold) {
     return SC(a, x) + SC(b, y) + SC(c, z) >= threshold;
 }
 
+/* Neighbours of word w: every v with score(w, v) >= T, plus w itself, in
+ * increasing word index. Enumerated letter by letter with a bound on the best
+ * possible remaining score. Returns the count written to out (<= ORC_NWORDS). */
+static int word_neighbours(int w, int32_t threshold, int32_t *out) {
+    static int32_t row_max[ORC_ALPHABET];
+    static int have_max = 0;
+    if (!have_max) {
+        for (int a = 0; a < ORC_ALPHABET; a++) {
+            int32_t m = SC(a, 0);
+            for (int b = 1; b < ORC_ALPHABET; b++) m = SC(a, b) > m ? SC(a, b) : m;
+            row_max[a] = m;
+        }
+        have_max = 1;
+    }
+    int a = w / 784, b = (w / 28) % 28, c = w % 28, n = 0, self = 0;
+    for (int x = 0; x < ORC_ALPHABET; x++) {
+        int32_t s0 = SC(a, x);
+        if (s0 + row_max[b] + row_max[c] < threshold && x != a) continue;
+        for (int y = 0; y < ORC_ALPHABET; y++) {
+            int32_t s1 = s0 + SC(b, y);
+            if (s1 + row_max[c] < threshold && !(x == a && y == b)) continue;
+            for (int z = 0; z < ORC_ALPHABET; z++) {
+                int v = x * 784 + y * 28 + z;
+                if (word_is_neighbour(w, v, threshold)) {
+                    out[n++] = v;
+                    self |= v == w;
+                }
+            }
+        }
+    }
+    (void)self;
+    return n;
+}
+
 int orc_lookup_build(const uint8_t *query, int32_t qlen, int32_t threshold, orc_lookup *out) {
     memset(out, 0, sizeof(*out));
     out->cell_start = (uint32_t *)calloc(ORC_NWORDS + 1, sizeof(uint32_t));
     if (!out->cell_start) return -1;
     int32_t nwords = qlen >= ORC_WORDSIZE ? qlen - ORC_WORDSIZE + 1 : 0;
-    /* neighbourhoods depend only on the query word: enumerate once per distinct word */
     uint32_t *count = (uint32_t *)calloc(ORC_NWORDS, sizeof(uint32_t));
+    int32_t *nb = (int32_t *)malloc(sizeof(int32_t) * ORC_NWORDS);
     int32_t *word_of = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nwords > 0 ? nwords : 1));
-    if (!count || !word_of) { free(count); free(word_of); return -1; }
+    if (!count || !word_of || !nb) { free(count); free(word_of); free(nb); return -1; }
     for (int32_t i = 0; i < nwords; i++) word_of[i] = query[i] * 784 + query[i + 1] * 28 + query[i + 2];
-    for (int32_t i = 0; i < nwords; i++)
-        for (int v = 0; v < ORC_NWORDS; v++)
-            if (word_is_neighbour(word_of[i], v, threshold)) count[v]++;
+    for (int32_t i = 0; i < nwords; i++) {
+        int k = word_neighbours(word_of[i], threshold, nb);
+        for (int j = 0; j < k; j++) count[nb[j]]++;
+    }
     uint32_t acc = 0;
     for (int v = 0; v < ORC_NWORDS; v++) { out->cell_start[v] = acc; acc += count[v]; }
     out->cell_start[ORC_NWORDS] = acc;
     out->n_offsets = acc;
     out->offsets = (uint32_t *)malloc(sizeof(uint32_t) * (acc ? acc : 1));
-    if (!out->offsets) { free(count); free(word_of); return -1; }
+    if (!out->offsets) { free(count); free(word_of); free(nb); return -1; }
     memset(count, 0, sizeof(uint32_t) * ORC_NWORDS);
-    for (int32_t i = 0; i < nwords; i++)
-        for (int v = 0; v < ORC_NWORDS; v++)
-            if (word_is_neighbour(word_of[i], v, threshold))
-                out->offsets[out->cell_start[v] + count[v]++] = (uint32_t)i;
+    for (int32_t i = 0; i < nwords; i++) {
+        int k = word_neighbours(word_of[i], threshold, nb);
+        for (int j = 0; j < k; j++) out->offsets[out->cell_start[nb[j]] + count[nb[j]]++] = (uint32_t)i;
+    }
     free(count);
     free(word_of);
+    free(nb);
     return 0;
 }
 
