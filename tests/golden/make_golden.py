@@ -1,0 +1,58 @@
+"""Regenerate the oracle regression fixtures in this directory.
+
+    python tests/golden/make_golden.py
+
+Each fixture holds a seeded synthetic case (query, residues, offsets), the
+search parameters, and the oracle's init hits and final HSPs for it. The
+reference ships no golden vectors for this path, so these pin the oracle
+against its own past output (regressions), while tests/test_oracle.py pins it
+against brute force and known answers.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "blaze-sc-ad_gb300")]
+
+import oracle  # noqa: E402
+from blaze103 import synth  # noqa: E402
+
+PARAM_KEYS = ["word_threshold", "window", "ungapped_xdrop", "ungapped_cutoff", "gap_open",
+              "gap_extend", "gapped_xdrop", "gapped_cutoff"]
+
+
+def cases():
+    w = synth.make_workload(0, scale=0.02)
+    yield "config0_scale002", w.queries[0], w.residues, w.offsets, (7_000_000, 20_000)
+    rng = np.random.default_rng(77)
+    alpha = np.array([1, 11, 17], dtype=np.uint8)
+    q = np.concatenate([alpha[rng.integers(0, 3, 120)], synth.random_residues(rng, 180)])
+    seqs = []
+    for i in range(120):
+        s = synth.random_residues(rng, int(rng.integers(40, 900)))
+        if i % 3 == 0:
+            s = np.concatenate([s, alpha[rng.integers(0, 3, int(rng.integers(40, 200)))]])
+        if i % 5 == 0:
+            s = np.concatenate([synth.mutate(rng, q[50:250], 0.5), s])
+        seqs.append(s)
+    off = np.zeros(len(seqs) + 1, dtype=np.uint64)
+    off[1:] = np.cumsum([len(s) for s in seqs])
+    yield "lowcomplexity_homologs", q, np.concatenate(seqs), off, (50_000_000, 150_000)
+
+
+def main():
+    for name, q, res, off, (dblen, dbn) in cases():
+        p = oracle.default_params(len(q), dblen, dbn)
+        hsps, inits = oracle.search_db(q, res, off, p, threads=4, want_inits=True)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), query=np.asarray(q, np.uint8),
+                            residues=np.asarray(res, np.uint8), offsets=off,
+                            params=np.array([p[k] for k in PARAM_KEYS], np.int32),
+                            db_len=np.int64(dblen), db_n=np.int64(dbn), hsps=hsps, inits=inits)
+        print(name, len(res), "residues", len(inits), "init hits", len(hsps), "HSPs")
+
+
+if __name__ == "__main__":
+    main()
