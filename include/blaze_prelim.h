@@ -161,6 +161,62 @@ int blaze_prelim_search(blaze_search *s, const uint8_t *query, int32_t length,
                         const blaze_params *p, blaze_hsp *out, uint64_t capacity,
                         uint64_t *n_hsps);
 
+/* ---------------------------------------------------------------------
+ * Gapped stage without device allocation.
+ *
+ * This entry point has no counterpart in the reference. It serves callers
+ * that cannot call cudaMalloc: applications whose own allocator already owns
+ * the device heap, and code that must not allocate because cudaMalloc and
+ * cudaFree can synchronize the whole device and stall other streams. The
+ * caller passes all inputs and outputs in its own device memory; the working
+ * memory (DP rows, ordered init hits, kept HSPs, counters) is one fixed
+ * array of BLAZE_NOALLOC_SCRATCH_BYTES compiled into the library, which every
+ * GPU that loads the library holds until the process exits.
+ *
+ * Input: the ungapped HSPs of each subject (d_init_hits, any order within a
+ * subject), grouped by d_subjects[i] = {subject index into d_offsets, count,
+ * first record}. Output: finished HSPs (score order within a subject,
+ * subjects in any order) in d_out; d_result[0] = HSPs produced (more than
+ * out_capacity means the output was cut), d_result[1] = status bits
+ * (0 = complete). Every subject must be at most max_subject_length residues
+ * long and carry at most max_init_hits_per_subject init hits; values above
+ * BLAZE_NOALLOC_MAX_SUBJECT_LENGTH / BLAZE_NOALLOC_MAX_INIT_HITS are rejected
+ * with BLAZE_ERR_LIMIT.
+ *
+ * The call only enqueues work on `stream` (a cudaStream_t); read d_result
+ * after synchronizing it. The first call on a device looks up the device
+ * address of the fixed array, so make that first call before any stream
+ * capture. All calls share the one array: calls whose work overlaps on the
+ * GPU (other streams, other threads) race and must be serialized by the
+ * caller. */
+#define BLAZE_NOALLOC_MAX_SUBJECT_LENGTH 4096u
+#define BLAZE_NOALLOC_MAX_INIT_HITS 128u
+#define BLAZE_NOALLOC_SCRATCH_BYTES (12u << 20)
+
+typedef struct blaze_dev_init_hit {
+    int32_t q_start, s_start, length, score;
+    int32_t q_trigger, s_trigger;
+} blaze_dev_init_hit;
+
+typedef struct blaze_dev_subject {
+    uint32_t subject;
+    uint32_t n_init_hits;
+    uint64_t first_init_hit;
+} blaze_dev_subject;
+
+typedef struct blaze_dev_hsp {
+    uint32_t subject;
+    int32_t score, q_start, q_end, s_start, s_end, q_gapped_start, s_gapped_start;
+} blaze_dev_hsp;
+
+int blaze_gapped_noalloc(const uint8_t *d_residues, const uint64_t *d_offsets,
+                         uint32_t max_subject_length, const uint8_t *d_query,
+                         int32_t query_length, const blaze_dev_init_hit *d_init_hits,
+                         const blaze_dev_subject *d_subjects, uint32_t n_subjects,
+                         uint32_t max_init_hits_per_subject, const blaze_params *p,
+                         blaze_dev_hsp *d_out, uint64_t out_capacity, uint64_t *d_result,
+                         void *stream);
+
 #ifdef __cplusplus
 }
 #endif
