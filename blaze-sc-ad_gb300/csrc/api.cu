@@ -39,6 +39,8 @@ struct blaze_query {
     uint64_t upload_bytes = 0;  // host->device bytes of the tables
     uint8_t *d_q = nullptr;
     uint32_t *d_cell_start = nullptr;
+    uint32_t *d_cell_pack = nullptr;
+    uint32_t *d_presence = nullptr;
     uint16_t *d_cell_off = nullptr;
     uint32_t n_off = 0;
 };
@@ -206,12 +208,25 @@ extern "C" int blaze_query_create(const blaze_db *db, const uint8_t *query, int3
     cudaError_t e = cudaMalloc(&q->d_q, static_cast<size_t>(length) + 64);
     if (e == cudaSuccess) e = cudaMalloc(&q->d_cell_start, sizeof(uint32_t) * (kWords + 1));
     if (e == cudaSuccess) e = cudaMalloc(&q->d_cell_off, sizeof(uint16_t) * std::max<uint32_t>(n_off, 1));
+    // packed cells (start << 8 | count, 255 = look at cell_start) and the
+    // word-presence bitset of the scan kernel
+    std::vector<uint32_t> pack(kWords), pres(kPresenceWords, 0u);
+    for (int w = 0; w < kWords; ++w) {
+        const uint32_t cnt = cs[w + 1] - cs[w];
+        pack[w] = (cs[w] << 8) | std::min<uint32_t>(cnt, 255u);
+        if (cnt) pres[w >> 5] |= 1u << (w & 31);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&q->d_cell_pack, sizeof(uint32_t) * kWords);
+    if (e == cudaSuccess) e = cudaMalloc(&q->d_presence, sizeof(uint32_t) * kPresenceWords);
+    if (e == cudaSuccess) e = cudaMemcpy(q->d_cell_pack, pack.data(), sizeof(uint32_t) * kWords, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(q->d_presence, pres.data(), sizeof(uint32_t) * kPresenceWords, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(q->d_q, query, length, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(q->d_q + length, 0, 64);
     if (e == cudaSuccess) e = cudaMemcpy(q->d_cell_start, cs.data(), sizeof(uint32_t) * (kWords + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n_off) e = cudaMemcpy(q->d_cell_off, offs, sizeof(uint16_t) * n_off, cudaMemcpyHostToDevice);
     std::free(offs);
-    q->upload_bytes = static_cast<uint64_t>(length) + sizeof(uint32_t) * (kWords + 1) + sizeof(uint16_t) * n_off;
+    q->upload_bytes = static_cast<uint64_t>(length) + sizeof(uint32_t) * (2 * kWords + 1 + kPresenceWords) +
+                      sizeof(uint16_t) * n_off;
     if (e != cudaSuccess) {
         last_cuda_error(e);
         blaze_query_free(q);
@@ -226,6 +241,8 @@ extern "C" int blaze_query_free(blaze_query *q) {
     cudaSetDevice(q->device);
     if (q->d_q) cudaFree(q->d_q);
     if (q->d_cell_start) cudaFree(q->d_cell_start);
+    if (q->d_cell_pack) cudaFree(q->d_cell_pack);
+    if (q->d_presence) cudaFree(q->d_presence);
     if (q->d_cell_off) cudaFree(q->d_cell_off);
     delete q;
     return BLAZE_OK;
@@ -291,8 +308,9 @@ static int check_params(const blaze_params *p) {
 }
 
 // One pass of both stages; fills s->h_cnt.
-static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p, uint32_t diag_entries,
-                    int warps_per_block, int scan_blocks, size_t smem) {
+static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p, const ScanLayout &lay,
+                    int scan_blocks) {
+    const int warps_per_block = lay.warps_per_block;
     blaze_db *db = s->db;
     const size_t scan_warps = static_cast<size_t>(scan_blocks) * warps_per_block;
     const size_t gapped_warps = static_cast<size_t>(s->gapped_blocks) * kGappedWarpsPerBlock;
@@ -315,11 +333,18 @@ static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p
     sa.q = q->d_q;
     sa.qlen = q->qlen;
     sa.cell_start = q->d_cell_start;
+    sa.cell_pack = q->d_cell_pack;
+    sa.presence = q->d_presence;
     sa.cell_off = q->d_cell_off;
     sa.window = p->window;
     sa.xdrop = p->ungapped_xdrop;
     sa.cutoff = p->ungapped_cutoff;
-    sa.diag_mask = diag_entries - 1;
+    sa.diag_entries = lay.diag_entries;
+    sa.diag_magic = lay.diag_magic;
+    sa.diag_bytes = lay.diag_bytes;
+    sa.stage_bytes = lay.stage_bytes;
+    sa.query_smem_bytes = lay.query_smem_bytes;
+    sa.warp_smem_bytes = lay.warp_smem_bytes;
     sa.scratch = s->scratch.p;
     sa.scratch_cap = s->scratch_cap;
     sa.init_out = s->init_out.p;
@@ -327,7 +352,7 @@ static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p
     sa.work = s->work.p;
     sa.work_cap = s->work.n;
     sa.cnt = s->d_cnt;
-    BLAZE_CUDA_TRY(launch_scan(sa, scan_blocks, warps_per_block, smem, s->stream));
+    BLAZE_CUDA_TRY(launch_scan(sa, scan_blocks, warps_per_block, lay.smem_bytes, s->stream));
     BLAZE_CUDA_TRY(cudaEventRecord(s->ev[2], s->stream));
 
     GappedArgs ga{};
@@ -371,21 +396,18 @@ extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const bla
     s->stats.h2d_bytes = q->upload_bytes;
     if (n_hsps) *n_hsps = 0;
 
-    uint32_t entries = 1;
-    while (entries < static_cast<uint32_t>(q->qlen + p->window)) entries <<= 1;
-    int wpb = kScanWarpsPerBlock;
-    constexpr size_t kSmemBudget = 200 * 1024;
-    while (wpb > 1 && scan_smem_bytes(entries, wpb) > kSmemBudget) --wpb;
-    const size_t smem = scan_smem_bytes(entries, wpb);
-    if (smem > 227 * 1024) return BLAZE_ERR_LIMIT;
+    constexpr size_t kSmemBudget = 220 * 1024;
+    const ScanLayout lay = scan_layout(q->qlen, p->window, kScanStageBytes, kSmemBudget);
+    if (lay.smem_bytes > 227 * 1024) return BLAZE_ERR_LIMIT;
     int per_sm = 0;
-    BLAZE_CUDA_TRY(scan_occupancy(wpb, smem, &per_sm));
-    const int scan_blocks = s->n_sm * std::max(per_sm, 1);
+    BLAZE_CUDA_TRY(scan_occupancy(lay.warps_per_block, lay.smem_bytes, &per_sm));
+    if (per_sm < 1) return BLAZE_ERR_LIMIT;
+    const int scan_blocks = s->n_sm * per_sm;
 
     DevCounters c{};
     BLAZE_CUDA_TRY(cudaEventRecord(s->ev[0], s->stream));
     for (int attempt = 0;; ++attempt) {
-        if ((rc = run_pass(s, q, p, entries, wpb, scan_blocks, smem)) != BLAZE_OK) return rc;
+        if ((rc = run_pass(s, q, p, lay, scan_blocks)) != BLAZE_OK) return rc;
         c = *s->h_cnt;
         {
             float ms = 0.f;

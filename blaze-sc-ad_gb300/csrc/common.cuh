@@ -18,10 +18,15 @@ constexpr int32_t kNeg = INT32_MIN / 2;  // "minus infinity" of the gapped DP
 constexpr int kWarp = 32;
 
 // Word-finder tuning (per warp of the scan kernel).
-constexpr int kDeferCap = 128;  // deferred hits per buffer (two buffers)
-constexpr int kSeedCap = 128;   // queued two-hit seeds (>= kDeferCap)
-constexpr int kScanWarpsPerBlock = 8;
+constexpr int kDeferCap = 64;   // deferred hits per buffer (two buffers)
+constexpr int kSeedCap = 64;    // queued two-hit seeds (>= kDeferCap)
+constexpr int kScanMaxWarpsPerBlock = 32;
 constexpr int kGappedWarpsPerBlock = 4;
+constexpr int kPresenceWords = (kWords + 31) / 32;                     // 686
+constexpr size_t kScanMatBytes = kAlphabet * kAlphabet;               // int8 matrix, 784
+constexpr size_t kScanPresenceBytes = (kPresenceWords * 4 + 15) & ~15; // 2752
+constexpr int32_t kQuerySmemMax = 8192;      // queries up to this length live in shared memory
+constexpr uint32_t kScanStageBytes = 2048;   // subjects up to this length are staged
 
 // An ungapped HSP that reached the ungapped cutoff (NCBI BlastInitHSP analog).
 struct InitHit {
@@ -73,9 +78,13 @@ struct ScanArgs {
     const uint8_t *q;          // query residues
     int32_t qlen;
     const uint32_t *cell_start;  // kWords + 1
+    const uint32_t *cell_pack;   // kWords: start << 8 | min(count, 255)
+    const uint32_t *presence;    // kPresenceWords: bit w set when word w has hits
     const uint16_t *cell_off;    // query offsets per cell, ascending
     int32_t window, xdrop, cutoff;
-    uint32_t diag_mask;        // diagonal table entries - 1 (power of two >= qlen + window)
+    uint32_t diag_entries;       // >= qlen + window
+    uint32_t diag_magic;         // floor(2^32 / diag_entries) + 1
+    uint32_t diag_bytes, stage_bytes, query_smem_bytes, warp_smem_bytes;
     InitHit *scratch;          // per warp: scratch_cap records
     uint32_t scratch_cap;
     InitHit *init_out;
@@ -104,11 +113,18 @@ struct GappedArgs {
     DevCounters *cnt;
 };
 
-// Launchers (kernels.cu).
+// Shared-memory layout of the scan kernel for one query.
+struct ScanLayout {
+    uint32_t diag_entries, diag_magic, diag_bytes, stage_bytes, query_smem_bytes, warp_smem_bytes;
+    int warps_per_block;
+    size_t smem_bytes;
+};
+
+// Launchers (scan.cu, kernels.cu).
+ScanLayout scan_layout(int32_t qlen, int32_t window, uint32_t stage_bytes, size_t smem_budget);
 cudaError_t launch_scan(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem, cudaStream_t st);
-cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st);
-size_t scan_smem_bytes(uint32_t diag_entries, int warps_per_block);
 cudaError_t scan_occupancy(int warps_per_block, size_t smem, int *blocks_per_sm);
+cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st);
 cudaError_t gapped_occupancy(int *blocks_per_sm);
 
 // Host helpers (host.cpp).

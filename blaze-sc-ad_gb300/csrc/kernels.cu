@@ -1,18 +1,15 @@
-// kernels.cu -- the two device stages of the BLASTP preliminary search on
-// GB300 (sm_103a). Integer work only: no tensor cores, no floating point.
+// kernels.cu -- the gapped stage of the BLASTP preliminary search on GB300
+// (sm_103a). Integer work only: no tensor cores, no floating point. (The
+// word finder, two-hit and ungapped stage is scan.cu.)
 //
-//   scan_kernel    word lookup -> two-hit seeds (window 40) -> ungapped X-drop;
-//                  one warp per subject, persistent warps pull subjects from a
-//                  device cursor, longest first. Publishes the subject's
-//                  ungapped HSPs (init hits) and a work item.
 //   gapped_kernel  one warp per work item: orders the init hits, skips those
 //                  contained in kept HSPs, runs the left and right score-only
 //                  X-drop DP row-parallel across the warp, then purges common
 //                  endpoints and sorts the subject's HSP list.
 //
-// Reference counterparts: gpuBLAZE_full (BLAZE_gpu/gpuBLAZE.cu:885-1252) and
-// gpuBLAZE_everything (gpuBLAZE.cu:1254-1397); unlike those (a filter whose
-// survivors the CPU re-searches) these produce the final HSPs.
+// Reference counterpart: gpuBLAZE_everything (BLAZE_gpu/gpuBLAZE.cu:1254-1397);
+// unlike that filter (whose survivors the CPU re-searches) this kernel
+// produces the final HSPs.
 #include <cstdint>
 
 #include "common.cuh"
@@ -26,336 +23,9 @@ __device__ const int32_t g_blosum[kAlphabet * kAlphabet] = {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr uint32_t kFlagBit = 0x80000000u;  // diagonal: an extension ran right
-constexpr uint32_t kPendBit = 0x40000000u;  // diagonal: a seed waits for its extension
-constexpr uint32_t kValMask = 0x3fffffffu;
-constexpr uint32_t kBaseReset = 1u << 28;
-
-__device__ __forceinline__ unsigned lanemask_lt() {
-    unsigned m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
 
 __device__ __forceinline__ void load_matrix(int32_t *mat) {
     for (int i = threadIdx.x; i < kAlphabet * kAlphabet; i += blockDim.x) mat[i] = g_blosum[i];
-}
-
-// ------------------------------------------------------------------------
-// Ungapped extension (scalar, one lane per seed). Same walks as the oracle:
-// left from the end of the best word prefix, right only when the left walk
-// reached the first hit (BLAZE_gpu/gpuBLAZE.cu:1096-1152 is the warp form).
-
-__device__ int32_t extend_left(const uint8_t *__restrict__ q, const uint8_t *__restrict__ s,
-                               int32_t q_off, int32_t s_off, int32_t xdrop, const int32_t *mat,
-                               int32_t *length) {
-    const int32_t n = min(s_off, q_off);
-    int32_t best_i = n + 1, score = 0, maxscore = 0;
-    const uint8_t *qq = q + q_off, *ss = s + s_off;
-    for (int32_t k = 0; k <= n; ++k) {
-        score += mat[qq[-k] * kAlphabet + ss[-k]];
-        if (score > maxscore) {
-            maxscore = score;
-            best_i = n - k;
-        }
-        if (maxscore - score >= xdrop) break;
-    }
-    *length = n - best_i + 1;
-    return maxscore;
-}
-
-__device__ int32_t extend_right(const uint8_t *__restrict__ q, int32_t qlen,
-                                const uint8_t *__restrict__ s, int32_t slen, int32_t q_off,
-                                int32_t s_off, int32_t xdrop, int32_t maxscore, const int32_t *mat,
-                                int32_t *length, int32_t *s_last_off) {
-    const int32_t n = min(slen - s_off, qlen - q_off);
-    int32_t best_i = -1, score = maxscore, i;
-    for (i = 0; i < n; ++i) {
-        score += mat[q[q_off + i] * kAlphabet + s[s_off + i]];
-        if (score > maxscore) {
-            maxscore = score;
-            best_i = i;
-        }
-        if (score <= 0 || maxscore - score >= xdrop) break;
-    }
-    *length = best_i + 1;
-    *s_last_off = s_off + i;
-    return maxscore;
-}
-
-__device__ int32_t extend_two_hit(const uint8_t *__restrict__ q, int32_t qlen,
-                                  const uint8_t *__restrict__ s, int32_t slen, int32_t s_left_off,
-                                  int32_t s_off, int32_t q_off, int32_t xdrop, const int32_t *mat,
-                                  int32_t *hsp_q, int32_t *hsp_s, int32_t *hsp_len,
-                                  int32_t *right_extend, int32_t *s_last_off) {
-    int32_t score = 0, left_score = 0, right_d = 0, left_d = 0, right_score = 0;
-#pragma unroll
-    for (int32_t i = 0; i < kWordSize; ++i) {
-        score += mat[q[q_off + i] * kAlphabet + s[s_off + i]];
-        if (score > left_score) {
-            left_score = score;
-            right_d = i + 1;
-        }
-    }
-    const int32_t q_right = q_off + right_d, s_right = s_off + right_d;
-    left_score = extend_left(q, s, q_right - 1, s_right - 1, xdrop, mat, &left_d);
-    right_d = 0;
-    *right_extend = 0;
-    *s_last_off = s_right;
-    if (left_d >= s_right - s_left_off) {
-        *right_extend = 1;
-        right_score = extend_right(q, qlen, s, slen, q_right, s_right, xdrop, left_score, mat,
-                                   &right_d, s_last_off);
-    }
-    *hsp_q = q_right - left_d;
-    *hsp_s = s_right - left_d;
-    *hsp_len = left_d + right_d;
-    return max(left_score, right_score);
-}
-
-// ------------------------------------------------------------------------
-// Word finder state of one warp. The diagonal table holds, per diagonal
-// (s - q) mod table size, either the last recorded hit (biased by window and
-// by a running base so the table never needs clearing between subjects),
-// the same with kFlagBit after a right extension, or kPendBit | seed slot
-// while that diagonal's extension is queued. A table of at least
-// qlen + window entries cannot mix two diagonals that both matter.
-
-struct WarpFinder {
-    uint32_t *diag;
-    uint2 *defer;     // two buffers of kDeferCap deferred hits {s, q}, arrival order
-    int4 *seeds;      // {q, s, s_left_off, table index}
-    int n_defer, n_seed, sel;
-    uint32_t base;
-    uint32_t n_init;
-    const uint8_t *sub;
-    int32_t slen;
-    InitHit *scratch;
-    unsigned long long extensions;
-};
-
-enum : int { kActNone = 0, kActSet = 1, kActSeed = 2, kActDefer = 3 };
-
-// Runs up to 32 hits (one per lane, lanes in hit order) through the two-hit
-// logic. Hits on the same diagonal are taken in lane order; a hit whose
-// diagonal waits on an extension is appended to the deferred list.
-__device__ __forceinline__ void process_batch(WarpFinder &wf, const ScanArgs &a, bool valid,
-                                              int32_t s, int32_t q) {
-    const uint32_t d = static_cast<uint32_t>(s - q) & a.diag_mask;
-    if (__ballot_sync(kFull, valid) == 0) return;
-    const unsigned lt = lanemask_lt();
-    const unsigned peers = __match_any_sync(kFull, valid ? d : 0xffffffffu);
-    const unsigned rank = valid ? __popc(peers & lt) : 0u;
-    const unsigned max_rank = __reduce_max_sync(kFull, rank);
-    for (unsigned r = 0; r <= max_rank; ++r) {
-        int act = kActNone;
-        uint32_t newv = 0;
-        int32_t s_left = 0;
-        if (valid && rank == r) {
-            const uint32_t e = wf.diag[d];
-            if (e & kPendBit) {
-                act = kActDefer;
-            } else {
-                const int32_t last = static_cast<int32_t>(e & kValMask) - a.window - static_cast<int32_t>(wf.base);
-                if (e & kFlagBit) {
-                    if (s >= last) {  // past the last extension: start over from this hit
-                        act = kActSet;
-                        newv = static_cast<uint32_t>(s + a.window) + wf.base;
-                    }
-                } else {
-                    const int32_t diff = s - last;
-                    if (diff >= a.window) {
-                        act = kActSet;
-                        newv = static_cast<uint32_t>(s + a.window) + wf.base;
-                    } else if (diff >= kWordSize) {
-                        act = kActSeed;
-                        s_left = last + kWordSize;
-                    }
-                }
-            }
-        }
-        const unsigned dm = __ballot_sync(kFull, act == kActDefer);
-        if (act == kActDefer)
-            wf.defer[wf.sel * kDeferCap + wf.n_defer + __popc(dm & lt)] = make_uint2(static_cast<uint32_t>(s), static_cast<uint32_t>(q));
-        wf.n_defer += __popc(dm);
-        const unsigned sm = __ballot_sync(kFull, act == kActSeed);
-        if (act == kActSeed) {
-            const int slot = wf.n_seed + __popc(sm & lt);
-            wf.seeds[slot] = make_int4(q, s, s_left, static_cast<int32_t>(d));
-            wf.diag[d] = kPendBit | static_cast<uint32_t>(slot);
-        }
-        wf.n_seed += __popc(sm);
-        if (act == kActSet) wf.diag[d] = newv;
-        __syncwarp();
-    }
-}
-
-// Extends every queued seed (one lane each), settles their diagonals, keeps
-// those reaching the ungapped cutoff, then replays the deferred hits; repeats
-// until no seed and no deferred hit is left.
-__device__ void flush(WarpFinder &wf, const ScanArgs &a, const int32_t *mat) {
-    const int lane = threadIdx.x & 31;
-    const unsigned lt = lanemask_lt();
-    while (wf.n_seed > 0 || wf.n_defer > 0) {
-        for (int c = 0; c < wf.n_seed; c += 32) {
-            const int i = c + lane;
-            bool pass = false;
-            int32_t hq = 0, hs = 0, hl = 0, score = 0;
-            int4 sd = make_int4(0, 0, 0, 0);
-            if (i < wf.n_seed) {
-                sd = wf.seeds[i];
-                int32_t rext, slast;
-                score = extend_two_hit(a.q, a.qlen, wf.sub, wf.slen, sd.z, sd.y, sd.x, a.xdrop, mat,
-                                       &hq, &hs, &hl, &rext, &slast);
-                wf.diag[sd.w] = rext ? (kFlagBit | (static_cast<uint32_t>(slast - (kWordSize - 1) + a.window) + wf.base))
-                                     : (static_cast<uint32_t>(sd.y + a.window) + wf.base);
-                pass = score >= a.cutoff;
-            }
-            const unsigned pm = __ballot_sync(kFull, pass);
-            if (pass) {
-                const uint32_t pos = wf.n_init + __popc(pm & lt);
-                if (pos < a.scratch_cap) {
-                    InitHit h;
-                    h.q_start = hq; h.s_start = hs; h.len = hl; h.score = score;
-                    h.q_trig = sd.x; h.s_trig = sd.y;
-                    wf.scratch[pos] = h;
-                }
-            }
-            wf.n_init += __popc(pm);
-        }
-        wf.extensions += static_cast<unsigned long long>(wf.n_seed);
-        wf.n_seed = 0;
-        __syncwarp();
-        if (wf.n_defer > 0) {
-            const int old = wf.sel, n_old = wf.n_defer;
-            wf.sel ^= 1;
-            wf.n_defer = 0;
-            for (int c = 0; c < n_old; c += 32) {
-                const int i = c + lane;
-                const bool v = i < n_old;
-                const uint2 h = v ? wf.defer[old * kDeferCap + i] : make_uint2(0u, 0u);
-                process_batch(wf, a, v, static_cast<int32_t>(h.x), static_cast<int32_t>(h.y));
-            }
-        }
-    }
-}
-
-__global__ void __launch_bounds__(kScanWarpsPerBlock * 32)
-scan_kernel(const ScanArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    int32_t *mat = reinterpret_cast<int32_t *>(smem);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t entries = a.diag_mask + 1;
-    const size_t per_warp = static_cast<size_t>(entries) * 4 + 2 * kDeferCap * sizeof(uint2) + kSeedCap * sizeof(int4);
-    unsigned char *mine = smem + kAlphabet * kAlphabet * sizeof(int32_t) + warp * per_warp;
-    load_matrix(mat);
-
-    WarpFinder wf;
-    wf.diag = reinterpret_cast<uint32_t *>(mine);
-    wf.defer = reinterpret_cast<uint2 *>(mine + static_cast<size_t>(entries) * 4);
-    wf.seeds = reinterpret_cast<int4 *>(wf.defer + 2 * kDeferCap);
-    wf.n_defer = wf.n_seed = wf.sel = 0;
-    wf.base = 0;
-    wf.extensions = 0;
-    const unsigned long long gwarp = (static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    wf.scratch = a.scratch + gwarp * a.scratch_cap;
-    for (uint32_t i = lane; i < entries; i += 32) wf.diag[i] = 0;
-    __syncthreads();
-
-    unsigned long long word_hits = 0, residues = 0;
-    const unsigned lt = lanemask_lt();
-    for (;;) {
-        unsigned long long t = 0;
-        if (lane == 0) t = atomicAdd(&a.cnt->next_scan, 1ull);
-        t = __shfl_sync(kFull, t, 0);
-        if (t >= a.n_subj) break;
-        const uint32_t subj = a.n_subj - 1 - static_cast<uint32_t>(t);
-        const uint64_t o0 = a.off[subj];
-        wf.slen = static_cast<int32_t>(a.off[subj + 1] - o0);
-        wf.sub = a.res + o0;
-        wf.n_init = 0;
-        residues += static_cast<unsigned long long>(wf.slen);
-        const int32_t nwords = wf.slen - (kWordSize - 1);
-        for (int32_t tb = 0; tb < nwords; tb += 32) {
-            const int32_t p = tb + lane;
-            uint32_t cs = 0, cnt = 0;
-            if (p < nwords) {
-                const int w = wf.sub[p] * 784 + wf.sub[p + 1] * 28 + wf.sub[p + 2];
-                cs = __ldg(a.cell_start + w);
-                cnt = __ldg(a.cell_start + w + 1) - cs;
-            }
-            uint32_t incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t x = __shfl_up_sync(kFull, incl, o);
-                if (lane >= o) incl += x;
-            }
-            const uint32_t total = __shfl_sync(kFull, incl, 31);
-            const uint32_t excl = incl - cnt;
-            word_hits += total;
-            for (uint32_t kb = 0; kb < total; kb += 32) {
-                const uint32_t k = kb + lane;
-                // owner = the last lane whose first hit index is <= k
-                int lo = 0;
-#pragma unroll
-                for (int step = 16; step >= 1; step >>= 1) {
-                    const uint32_t ev = __shfl_sync(kFull, excl, lo + step);
-                    if (ev <= k) lo += step;
-                }
-                const uint32_t hcs = __shfl_sync(kFull, cs, lo);
-                const uint32_t hex = __shfl_sync(kFull, excl, lo);
-                const bool hv = k < total;
-                const int32_t qo = hv ? static_cast<int32_t>(__ldg(a.cell_off + hcs + (k - hex))) : 0;
-                process_batch(wf, a, hv, tb + lo, qo);
-                if (wf.n_seed >= 32 || wf.n_defer > kDeferCap - 32) flush(wf, a, mat);
-            }
-        }
-        flush(wf, a, mat);
-
-        // publish this subject's init hits as one contiguous block
-        if (wf.n_init > 0) {
-            if (wf.n_init > a.scratch_cap) {
-                if (lane == 0) {
-                    atomicAdd(&a.cnt->overflow_subjects, 1u);
-                    atomicMax(&a.cnt->max_init_needed, wf.n_init);
-                }
-            } else {
-                unsigned long long first = 0, wi = 0;
-                if (lane == 0) {
-                    first = atomicAdd(&a.cnt->init_count, static_cast<unsigned long long>(wf.n_init));
-                    wi = atomicAdd(&a.cnt->work_count, 1ull);
-                }
-                first = __shfl_sync(kFull, first, 0);
-                wi = __shfl_sync(kFull, wi, 0);
-                if (first + wf.n_init > a.init_cap || wi >= a.work_cap) {
-                    if (lane == 0)
-                        atomicOr(&a.cnt->flags, first + wf.n_init > a.init_cap ? kFlagInitArrayFull : kFlagWorkArrayFull);
-                } else {
-                    for (uint32_t i = lane; i < wf.n_init; i += 32) a.init_out[first + i] = wf.scratch[i];
-                    if (lane == 0) {
-                        WorkItem w;
-                        w.subject = subj;
-                        w.n_init = wf.n_init;
-                        w.first = first;
-                        a.work[wi] = w;
-                    }
-                }
-            }
-        }
-        wf.base += static_cast<uint32_t>(wf.slen + a.window);
-        if (wf.base > kBaseReset) {
-            __syncwarp();
-            for (uint32_t i = lane; i < entries; i += 32) wf.diag[i] = 0;
-            wf.base = 0;
-        }
-        __syncwarp();
-    }
-    (void)lt;
-    if (lane == 0) {
-        atomicAdd(&a.cnt->word_hits, word_hits);
-        atomicAdd(&a.cnt->residues, residues);
-        atomicAdd(&a.cnt->extensions, wf.extensions);
-    }
 }
 
 // ------------------------------------------------------------------------
@@ -666,30 +336,9 @@ gapped_kernel(const GappedArgs a) {
 
 }  // namespace
 
-size_t scan_smem_bytes(uint32_t diag_entries, int warps_per_block) {
-    const size_t per_warp = static_cast<size_t>(diag_entries) * 4 + 2 * kDeferCap * sizeof(uint2) + kSeedCap * sizeof(int4);
-    return kAlphabet * kAlphabet * sizeof(int32_t) + per_warp * static_cast<size_t>(warps_per_block);
-}
-
-cudaError_t launch_scan(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem, cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    scan_kernel<<<n_blocks, warps_per_block * 32, smem, st>>>(a);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st) {
     gapped_kernel<<<n_blocks, kGappedWarpsPerBlock * 32, 0, st>>>(a);
     return cudaGetLastError();
-}
-
-cudaError_t scan_occupancy(int warps_per_block, size_t smem, int *blocks_per_sm) {
-    cudaError_t e = cudaFuncSetAttribute(scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, scan_kernel,
-                                                         warps_per_block * 32, smem);
 }
 
 cudaError_t gapped_occupancy(int *blocks_per_sm) {
