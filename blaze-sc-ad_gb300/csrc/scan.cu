@@ -148,52 +148,42 @@ enum : int { kActNone = 0, kActSet = 1, kActSeed = 2, kActDefer = 3 };
 // diagonal waits on an extension is appended to the deferred list.
 __device__ __forceinline__ void process_batch(WarpFinder &wf, const ScanArgs &a, bool valid,
                                               int32_t s, int32_t q) {
-    const uint32_t d = fast_mod(static_cast<uint32_t>(s - q + a.qlen), a.diag_entries, a.diag_magic);
     if (__ballot_sync(kFull, valid) == 0) return;
+    const uint32_t d = fast_mod(static_cast<uint32_t>(s - q + a.qlen), a.diag_entries, a.diag_magic);
     const unsigned lt = lanemask_lt();
     const unsigned peers = __match_any_sync(kFull, valid ? d : 0xffffffffu);
     const unsigned rank = valid ? __popc(peers & lt) : 0u;
     const unsigned max_rank = __reduce_max_sync(kFull, rank);
+    const uint32_t here = static_cast<uint32_t>(s + a.window) + wf.base;  // s, biased
     for (unsigned r = 0; r <= max_rank; ++r) {
-        int act = kActNone;
-        uint32_t newv = 0;
-        int32_t s_left = 0;
-        if (valid && rank == r) {
-            const uint32_t e = wf.diag[d];
-            if (e & kPendBit) {
-                act = kActDefer;
-            } else {
-                const int32_t last = static_cast<int32_t>(e & kValMask) - a.window - static_cast<int32_t>(wf.base);
-                if (e & kFlagBit) {
-                    if (s >= last) {  // past the last extension: start over from this hit
-                        act = kActSet;
-                        newv = static_cast<uint32_t>(s + a.window) + wf.base;
-                    }
-                } else {
-                    const int32_t diff = s - last;
-                    if (diff >= a.window) {
-                        act = kActSet;
-                        newv = static_cast<uint32_t>(s + a.window) + wf.base;
-                    } else if (diff >= kWordSize) {
-                        act = kActSeed;
-                        s_left = last + kWordSize;
-                    }
-                }
+        const bool mine = valid && rank == r;
+        const uint32_t e = mine ? wf.diag[d] : 0u;
+        const bool pend = (e & kPendBit) != 0u;
+        const bool flag = (e & kFlagBit) != 0u;
+        const int32_t last = static_cast<int32_t>(e & kValMask) - a.window - static_cast<int32_t>(wf.base);
+        const int32_t diff = s - last;
+        // flag set: hits inside the last extension are skipped, the first one
+        // past it starts over; otherwise a hit far from the last one starts
+        // over, one at distance [wordsize, window) triggers an extension, and
+        // an overlapping one is ignored
+        const bool defer = mine && pend;
+        const bool seed = mine && !pend && !flag && diff >= kWordSize && diff < a.window;
+        const bool set = mine && !pend && (flag ? s >= last : diff >= a.window);
+        if (set) wf.diag[d] = here;
+        const unsigned dm = __ballot_sync(kFull, defer);
+        const unsigned sm = __ballot_sync(kFull, seed);
+        if ((dm | sm) != 0u) {
+            if (defer)
+                wf.defer[wf.sel * kDeferCap + wf.n_defer + __popc(dm & lt)] =
+                    make_uint2(static_cast<uint32_t>(s), static_cast<uint32_t>(q));
+            if (seed) {
+                const int slot = wf.n_seed + __popc(sm & lt);
+                wf.seeds[slot] = make_int4(q, s, last + kWordSize, static_cast<int32_t>(d));
+                wf.diag[d] = kPendBit | static_cast<uint32_t>(slot);
             }
+            wf.n_defer += __popc(dm);
+            wf.n_seed += __popc(sm);
         }
-        const unsigned dm = __ballot_sync(kFull, act == kActDefer);
-        if (act == kActDefer)
-            wf.defer[wf.sel * kDeferCap + wf.n_defer + __popc(dm & lt)] =
-                make_uint2(static_cast<uint32_t>(s), static_cast<uint32_t>(q));
-        wf.n_defer += __popc(dm);
-        const unsigned sm = __ballot_sync(kFull, act == kActSeed);
-        if (act == kActSeed) {
-            const int slot = wf.n_seed + __popc(sm & lt);
-            wf.seeds[slot] = make_int4(q, s, s_left, static_cast<int32_t>(d));
-            wf.diag[d] = kPendBit | static_cast<uint32_t>(slot);
-        }
-        wf.n_seed += __popc(sm);
-        if (act == kActSet) wf.diag[d] = newv;
         __syncwarp();
     }
 }
@@ -253,7 +243,7 @@ __device__ void flush(WarpFinder &wf, const ScanArgs &a, const int8_t *mat) {
     }
 }
 
-__global__ void __launch_bounds__(kScanMaxWarpsPerBlock * 32)
+__global__ void __launch_bounds__(kScanMaxWarpsPerBlock * 32, 1)
 scan_kernel(const ScanArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -305,47 +295,53 @@ scan_kernel(const ScanArgs a) {
             wf.sub = a.res + o0;
         }
         const int32_t nwords = wf.slen - (kWordSize - 1);
-        // cell of the lane's position in tile tb (0 hits past the end)
-        auto cell_of = [&](int32_t tb, uint32_t &cs, uint32_t &cnt) {
-            const int32_t p = tb + lane;
-            cs = 0;
-            cnt = 0;
-            if (p < nwords) {
-                const int w = wf.sub[p] * 784 + wf.sub[p + 1] * 28 + wf.sub[p + 2];
-                if ((presence[w >> 5] >> (w & 31)) & 1u) {
-                    const uint32_t pk = __ldg(a.cell_pack + w);
-                    cs = pk >> 8;
-                    cnt = pk & 0xffu;
-                    if (cnt == 0xffu) cnt = __ldg(a.cell_start + w + 1) - cs;
-                }
+        // chunks of 128 word positions, four consecutive positions per lane
+        for (int32_t cb = 0; cb < nwords; cb += 4 * 32) {
+            const int32_t p0 = cb + 4 * lane;
+            int32_t r[6];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) r[j] = wf.sub[min(p0 + j, wf.slen - 1)];
+            uint32_t cs[4], cnt[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int w = r[j] * 784 + r[j + 1] * 28 + r[j + 2];
+                const bool present = p0 + j < nwords && ((presence[w >> 5] >> (w & 31)) & 1u);
+                const uint32_t pk = present ? __ldg(a.cell_pack + w) : 0u;
+                cs[j] = pk >> 8;
+                cnt[j] = pk & 0xffu;
+                if (cnt[j] == 0xffu) cnt[j] = __ldg(a.cell_start + w + 1) - cs[j];
             }
-        };
-        for (int32_t tb = 0; tb < nwords; tb += 32) {
-            uint32_t cs, cnt;
-            cell_of(tb, cs, cnt);
-            uint32_t incl = cnt;
+            const uint32_t mine_total = cnt[0] + cnt[1] + cnt[2] + cnt[3];
+            uint32_t incl = mine_total;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const uint32_t x = __shfl_up_sync(kFull, incl, o);
                 if (lane >= o) incl += x;
             }
             const uint32_t total = __shfl_sync(kFull, incl, 31);
-            const uint32_t excl = incl - cnt;
+            if (total == 0) continue;
             word_hits += total;
+            const uint32_t e0 = incl - mine_total, e1 = e0 + cnt[0], e2 = e1 + cnt[1], e3 = e2 + cnt[2];
             for (uint32_t kb = 0; kb < total; kb += 32) {
                 const uint32_t k = kb + lane;
-                // owner = the last lane whose first hit index is <= k
+                // owner lane: the last lane whose first hit index is <= k
                 int lo = 0;
 #pragma unroll
                 for (int step = 16; step >= 1; step >>= 1) {
-                    const uint32_t ev = __shfl_sync(kFull, excl, lo + step);
+                    const uint32_t ev = __shfl_sync(kFull, e0, lo + step);
                     if (ev <= k) lo += step;
                 }
-                const uint32_t hcs = __shfl_sync(kFull, cs, lo);
-                const uint32_t hex = __shfl_sync(kFull, excl, lo);
+                // owner position: the last of its four whose first hit is <= k
+                const uint32_t E0 = __shfl_sync(kFull, e0, lo), E1 = __shfl_sync(kFull, e1, lo);
+                const uint32_t E2 = __shfl_sync(kFull, e2, lo), E3 = __shfl_sync(kFull, e3, lo);
+                const uint32_t C0 = __shfl_sync(kFull, cs[0], lo), C1 = __shfl_sync(kFull, cs[1], lo);
+                const uint32_t C2 = __shfl_sync(kFull, cs[2], lo), C3 = __shfl_sync(kFull, cs[3], lo);
+                const int j = (k >= E1) + (k >= E2) + (k >= E3);
+                const uint32_t Ej = j == 0 ? E0 : j == 1 ? E1 : j == 2 ? E2 : E3;
+                const uint32_t Cj = j == 0 ? C0 : j == 1 ? C1 : j == 2 ? C2 : C3;
                 const bool hv = k < total;
-                const int32_t qo = hv ? static_cast<int32_t>(__ldg(a.cell_off + hcs + (k - hex))) : 0;
-                process_batch(wf, a, hv, tb + lo, qo);
+                const int32_t qo = hv ? static_cast<int32_t>(__ldg(a.cell_off + Cj + (k - Ej))) : 0;
+                process_batch(wf, a, hv, cb + 4 * lo + j, qo);
                 if (wf.n_seed >= 32 || wf.n_defer > kDeferCap - 32) flush(wf, a, mat);
             }
         }
