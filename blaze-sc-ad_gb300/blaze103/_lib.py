@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "libblaze103.so")
 # The exported entry points and their C signatures (kept in step with
 # include/blaze_prelim.h; tests check the two agree).
 EXPORTS = (
-    "blaze_status_string", "blaze_device_count", "blaze_db_create", "blaze_db_free",
+    "blaze_status_string", "blaze_last_cuda_error", "blaze_device_count", "blaze_db_create", "blaze_db_free",
     "blaze_db_info", "blaze_query_create", "blaze_query_free", "blaze_params_default",
     "blaze_search_create", "blaze_search_free", "blaze_search_run", "blaze_search_results",
     "blaze_search_stats", "blaze_search_init_hits", "blaze_prelim_search",
@@ -62,7 +62,13 @@ class BlazeStats(ctypes.Structure):
 class BlazeError(RuntimeError):
     def __init__(self, status: int, what: str):
         self.status = status
-        super().__init__(f"{what}: {status_string(status)} (status {status})")
+        detail = ""
+        if status == 2:  # BLAZE_ERR_CUDA
+            try:
+                detail = ": " + load().blaze_last_cuda_error().decode()
+            except OSError:
+                pass
+        super().__init__(f"{what}: {status_string(status)} (status {status}){detail}")
 
 
 _lib = None
@@ -83,6 +89,8 @@ def load(path: str | None = None):
     i32, u32 = ctypes.c_int32, ctypes.c_uint32
     L.blaze_status_string.argtypes = [ctypes.c_int]
     L.blaze_status_string.restype = ctypes.c_char_p
+    L.blaze_last_cuda_error.argtypes = []
+    L.blaze_last_cuda_error.restype = ctypes.c_char_p
     L.blaze_device_count.argtypes = [ctypes.POINTER(ctypes.c_int)]
     L.blaze_db_create.argtypes = [ctypes.c_int, u8p, u64p, u32, ctypes.POINTER(vp)]
     L.blaze_db_free.argtypes = [vp]
@@ -100,7 +108,7 @@ def load(path: str | None = None):
     L.blaze_prelim_search.argtypes = [vp, u8p, i32, ctypes.POINTER(BlazeParams), vp,
                                       ctypes.c_uint64, u64p]
     for name in EXPORTS:
-        if name != "blaze_status_string":
+        if name not in ("blaze_status_string", "blaze_last_cuda_error"):
             getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L

@@ -22,6 +22,8 @@ constexpr uint32_t kInitialScratchCap = 1024;             // init hits per subje
 
 void last_cuda_error(cudaError_t e) { g_last_cuda = e; }
 
+extern "C" const char *blaze_last_cuda_error(void) { return cudaGetErrorString(g_last_cuda); }
+
 struct blaze_db {
     int device = 0;
     uint8_t *d_res = nullptr;
@@ -397,10 +399,12 @@ extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const bla
     if (n_hsps) *n_hsps = 0;
 
     constexpr size_t kSmemBudget = 220 * 1024;
-    const ScanLayout lay = scan_layout(q->qlen, p->window, kScanStageBytes, kSmemBudget);
+    const bool qsmem = q->qlen <= kQuerySmemMax;
+    const ScanLayout lay = scan_layout(q->qlen, p->window, kScanStageBytes, kSmemBudget,
+                                       scan_max_warps_by_registers(qsmem));
     if (lay.smem_bytes > 227 * 1024) return BLAZE_ERR_LIMIT;
     int per_sm = 0;
-    BLAZE_CUDA_TRY(scan_occupancy(lay.warps_per_block, lay.smem_bytes, &per_sm));
+    BLAZE_CUDA_TRY(scan_occupancy(lay.query_smem_bytes != 0, lay.warps_per_block, lay.smem_bytes, &per_sm));
     if (per_sm < 1) return BLAZE_ERR_LIMIT;
     const int scan_blocks = s->n_sm * per_sm;
 

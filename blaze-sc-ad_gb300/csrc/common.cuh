@@ -121,9 +121,10 @@ struct ScanLayout {
 };
 
 // Launchers (scan.cu, kernels.cu).
-ScanLayout scan_layout(int32_t qlen, int32_t window, uint32_t stage_bytes, size_t smem_budget);
+ScanLayout scan_layout(int32_t qlen, int32_t window, uint32_t stage_bytes, size_t smem_budget, int max_warps);
 cudaError_t launch_scan(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem, cudaStream_t st);
-cudaError_t scan_occupancy(int warps_per_block, size_t smem, int *blocks_per_sm);
+cudaError_t scan_occupancy(bool query_in_smem, int warps_per_block, size_t smem, int *blocks_per_sm);
+int scan_max_warps_by_registers(bool query_in_smem);
 cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st);
 cudaError_t gapped_occupancy(int *blocks_per_sm);
 

@@ -109,6 +109,10 @@ typedef struct blaze_stats {
 
 const char *blaze_status_string(int status);
 
+/* Text of the last CUDA runtime error seen by this thread inside the library
+ * ("no error" when none); explains a BLAZE_ERR_CUDA status. */
+const char *blaze_last_cuda_error(void);
+
 /* Number of usable devices (0 when none). */
 int blaze_device_count(int *count);
 

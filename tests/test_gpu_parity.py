@@ -130,3 +130,16 @@ def test_invalid_inputs_rejected():
     assert e.value.status == 1
     ps.close()
     db.close()
+
+
+def test_query_longer_than_shared_copy():
+    # queries above 8192 residues are read from global memory by the word finder
+    rng = np.random.default_rng(9000)
+    q = synth.random_residues(rng, 9000)
+    seqs = [synth.random_residues(rng, int(L)) for L in synth.lognormal_lengths(rng, 300, 250, 0.82, 30, 3000)]
+    for i in range(0, len(seqs), 6):
+        s0 = int(rng.integers(0, len(q) - 300))
+        seqs[i] = np.concatenate([seqs[i], synth.mutate(rng, q[s0:s0 + 250], 0.5)])
+    res, off = concat(seqs)
+    got, _, _ = compare(q, res, off)
+    assert len(got) > 10
