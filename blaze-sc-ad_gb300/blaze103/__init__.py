@@ -24,11 +24,12 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import (HSP_DTYPE, INIT_DTYPE, BlazeError, BlazeParams, BlazeStats, check, load, u8ptr,
-                   u64ptr, status_string)
+from ._lib import (BATCH_HSP_DTYPE, HSP_DTYPE, INIT_DTYPE, BlazeError, BlazeParams, BlazeStats,
+                   BlazeTuning, check, load, u8ptr, u64ptr, status_string)
 
-__all__ = ["SeqSrc", "PrelimSearch", "HSPResults", "BlazeParams", "BlazeError", "HSP_DTYPE",
-           "default_params", "device_count", "load", "status_string"]
+__all__ = ["SeqSrc", "PrelimSearch", "HSPResults", "QueryBatch", "BlazeParams", "BlazeTuning",
+           "BlazeError", "HSP_DTYPE", "BATCH_HSP_DTYPE", "default_params", "device_count", "load",
+           "status_string"]
 
 
 def device_count() -> int:
@@ -139,6 +140,45 @@ class Query:
             pass
 
 
+class QueryBatch:
+    """Many queries resident on the device for one batched launch."""
+
+    def __init__(self, seq_src: SeqSrc, queries, word_threshold: int = 11):
+        self._lib = load()
+        qs = [_codes(q, "query") for q in queries]
+        if not qs:
+            raise ValueError("empty batch")
+        off = np.zeros(len(qs) + 1, dtype=np.uint64)
+        off[1:] = np.cumsum([len(q) for q in qs])
+        res = np.concatenate(qs)
+        h = ctypes.c_void_p()
+        check(self._lib.blaze_batch_create(seq_src.handle, u8ptr(res), u64ptr(off), len(qs),
+                                           int(word_threshold), ctypes.byref(h)), "blaze_batch_create")
+        self._h = h
+        self.lengths = [len(q) for q in qs]
+        n, b = ctypes.c_uint32(), ctypes.c_uint64()
+        check(self._lib.blaze_batch_info(h, ctypes.byref(n), ctypes.byref(b)), "blaze_batch_info")
+        self.device_bytes = b.value
+
+    def __len__(self):
+        return len(self.lengths)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.blaze_batch_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class PrelimSearch:
     """Runs the preliminary search stage against one SeqSrc (one CUDA stream)."""
 
@@ -186,6 +226,25 @@ class PrelimSearch:
             return HSPResults(self.results(), self.stats())
         finally:
             q.close()
+
+    def set_tuning(self, stage_bytes: int = 0, tile_subjects: int = 0, max_warps_per_block: int = 0):
+        t = BlazeTuning(int(stage_bytes), int(tile_subjects), int(max_warps_per_block))
+        check(self._lib.blaze_search_set_tuning(self._h, ctypes.byref(t)), "blaze_search_set_tuning")
+
+    def run_batch(self, batch: QueryBatch, params=None, evalue: float = 10.0) -> np.ndarray:
+        """Every query of the batch in one batched launch; returns
+        BATCH_HSP_DTYPE records grouped by query, then OID."""
+        if params is None:
+            params = [default_params(L, self.seq_src, evalue) for L in batch.lengths]
+        arr = (BlazeParams * len(params))(*params)
+        n = ctypes.c_uint64()
+        check(self._lib.blaze_search_run_batch(self._h, batch.handle, arr, ctypes.byref(n)),
+              "blaze_search_run_batch")
+        out = np.zeros(n.value, dtype=BATCH_HSP_DTYPE)
+        check(self._lib.blaze_search_batch_results(self._h, out.ctypes.data_as(ctypes.c_void_p),
+                                                   n.value, ctypes.byref(n)),
+              "blaze_search_batch_results")
+        return out
 
     def prelim_search(self, query, params: BlazeParams, capacity: int) -> np.ndarray:
         """The one-call C-ABI path with host buffers (blaze_prelim_search)."""

@@ -16,6 +16,8 @@ EXPORTS = (
     "blaze_db_info", "blaze_query_create", "blaze_query_free", "blaze_params_default",
     "blaze_search_create", "blaze_search_free", "blaze_search_run", "blaze_search_results",
     "blaze_search_stats", "blaze_search_init_hits", "blaze_prelim_search",
+    "blaze_batch_create", "blaze_batch_free", "blaze_batch_info", "blaze_search_run_batch",
+    "blaze_search_batch_results", "blaze_search_set_tuning",
 )
 
 HSP_DTYPE = np.dtype([
@@ -24,6 +26,9 @@ HSP_DTYPE = np.dtype([
     ("evalue", "<f8"),
 ])
 assert HSP_DTYPE.itemsize == 40
+BATCH_HSP_DTYPE = np.dtype([("query", "<u4"), ("reserved", "<u4")] + [
+    (n, HSP_DTYPE.fields[n][0]) for n in HSP_DTYPE.names])
+assert BATCH_HSP_DTYPE.itemsize == 48
 INIT_DTYPE = np.dtype([
     ("oid", "<u4"), ("q_start", "<i4"), ("s_start", "<i4"), ("length", "<i4"), ("score", "<i4"),
     ("q_trigger", "<i4"), ("s_trigger", "<i4"),
@@ -42,6 +47,11 @@ class BlazeParams(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {(k[:-1] if k.endswith("_") else k): getattr(self, k) for k, _ in self._fields_}
+
+
+class BlazeTuning(ctypes.Structure):
+    _fields_ = [("stage_bytes", ctypes.c_uint32), ("tile_subjects", ctypes.c_uint32),
+                ("max_warps_per_block", ctypes.c_uint32)]
 
 
 class BlazeStats(ctypes.Structure):
@@ -107,6 +117,12 @@ def load(path: str | None = None):
     L.blaze_search_init_hits.argtypes = [vp, vp, ctypes.c_uint64, u64p]
     L.blaze_prelim_search.argtypes = [vp, u8p, i32, ctypes.POINTER(BlazeParams), vp,
                                       ctypes.c_uint64, u64p]
+    L.blaze_batch_create.argtypes = [vp, u8p, u64p, u32, i32, ctypes.POINTER(vp)]
+    L.blaze_batch_free.argtypes = [vp]
+    L.blaze_batch_info.argtypes = [vp, ctypes.POINTER(u32), u64p]
+    L.blaze_search_run_batch.argtypes = [vp, vp, ctypes.POINTER(BlazeParams), u64p]
+    L.blaze_search_batch_results.argtypes = [vp, vp, ctypes.c_uint64, u64p]
+    L.blaze_search_set_tuning.argtypes = [vp, ctypes.POINTER(BlazeTuning)]
     for name in EXPORTS:
         if name not in ("blaze_status_string", "blaze_last_cuda_error"):
             getattr(L, name).restype = ctypes.c_int

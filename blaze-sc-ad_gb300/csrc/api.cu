@@ -86,7 +86,33 @@ struct blaze_search {
     std::vector<blaze_hsp> results;
     blaze_stats stats{};
     unsigned long long last_init_count = 0, last_work_count = 0;
+    bool last_batched = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // launch shape (blaze_search_set_tuning)
+    uint32_t stage_bytes = kScanStageBytes;
+    uint32_t tile_subjects = kDefaultTileSubjects;
+    uint32_t max_warps = 0;
+    // batched runs
+    unsigned long long work_cap = 0;
+    DevBuf<BatchQuery> bq;
+    DevBuf<const uint8_t *> bqptr;
+    DevBuf<int32_t> bqlen, bcut;
+    DevBuf<uint32_t> work_query, out_query;
+    uint32_t *h_outq = nullptr;  // pinned
+    size_t h_outq_n = 0;
+    std::vector<blaze_batch_hsp> batch_results;
+};
+
+struct blaze_batch {
+    int device = 0;
+    uint32_t n = 0;
+    int32_t threshold = 0;
+    std::vector<int32_t> qlen;
+    std::vector<uint64_t> res_off, off_off;  // per query: residues, hit lists
+    uint8_t *d_res = nullptr;
+    uint32_t *d_cell_start = nullptr, *d_cell_pack = nullptr, *d_presence = nullptr;
+    uint16_t *d_cell_off = nullptr;
+    uint64_t upload_bytes = 0, device_bytes = 0;
 };
 
 static bool valid_residues(const uint8_t *r, uint64_t n) {
@@ -270,12 +296,14 @@ extern "C" int blaze_search_create(blaze_db *db, blaze_search **out) {
     }
     s->gapped_blocks = s->n_sm * std::min(std::max(per_sm, 1), 8);
     s->init_cap = std::max<unsigned long long>(1ull << 20, db->n / 8);
+    s->work_cap = std::max<unsigned long long>(1ull << 20, db->n / 4);
     s->out_cap = std::max<unsigned long long>(1ull << 20, db->n / 16);
     // Starting capacities can be lowered (e.g. to exercise the grow-and-repeat
     // path); they grow on demand either way.
     if (const char *v = std::getenv("BLAZE_INITIAL_SCRATCH_CAP")) s->scratch_cap = std::max(1, std::atoi(v));
     if (const char *v = std::getenv("BLAZE_INITIAL_INIT_CAP")) s->init_cap = std::max(1, std::atoi(v));
     if (const char *v = std::getenv("BLAZE_INITIAL_OUT_CAP")) s->out_cap = std::max(1, std::atoi(v));
+    if (const char *v = std::getenv("BLAZE_INITIAL_WORK_CAP")) s->work_cap = std::max(1, std::atoi(v));
     *out = s;
     return BLAZE_OK;
 }
@@ -291,6 +319,13 @@ extern "C" int blaze_search_free(blaze_search *s) {
     s->saved.release();
     s->out.release();
     s->dp.release();
+    s->bq.release();
+    s->bqptr.release();
+    s->bqlen.release();
+    s->bcut.release();
+    s->work_query.release();
+    s->out_query.release();
+    if (s->h_outq) cudaFreeHost(s->h_outq);
     if (s->d_cnt) cudaFree(s->d_cnt);
     if (s->h_cnt) cudaFreeHost(s->h_cnt);
     if (s->h_out) cudaFreeHost(s->h_out);
@@ -309,20 +344,34 @@ static int check_params(const blaze_params *p) {
     return BLAZE_OK;
 }
 
+// What one run searches: one query, or a batch with one parameter set per
+// query.
+struct RunSpec {
+    const blaze_query *q = nullptr;
+    const blaze_batch *b = nullptr;
+    const blaze_params *p = nullptr;
+};
+
 // One pass of both stages; fills s->h_cnt.
-static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p, const ScanLayout &lay,
-                    int scan_blocks) {
+static int run_pass(blaze_search *s, const RunSpec &r, const ScanLayout &lay, int scan_blocks) {
     const int warps_per_block = lay.warps_per_block;
     blaze_db *db = s->db;
+    const blaze_params *p = r.p;
+    const bool batched = r.b != nullptr;
     const size_t scan_warps = static_cast<size_t>(scan_blocks) * warps_per_block;
     const size_t gapped_warps = static_cast<size_t>(s->gapped_blocks) * kGappedWarpsPerBlock;
+    const size_t work_cap = batched ? s->work_cap : std::max<uint32_t>(db->n, 1);
     int rc;
     if ((rc = s->scratch.ensure(scan_warps * s->scratch_cap)) != BLAZE_OK) return rc;
     if ((rc = s->sorted.ensure(gapped_warps * s->scratch_cap)) != BLAZE_OK) return rc;
     if ((rc = s->saved.ensure(gapped_warps * s->scratch_cap)) != BLAZE_OK) return rc;
     if ((rc = s->init_out.ensure(s->init_cap)) != BLAZE_OK) return rc;
-    if ((rc = s->work.ensure(std::max<uint32_t>(db->n, 1))) != BLAZE_OK) return rc;
+    if ((rc = s->work.ensure(work_cap)) != BLAZE_OK) return rc;
     if ((rc = s->out.ensure(s->out_cap)) != BLAZE_OK) return rc;
+    if (batched) {
+        if ((rc = s->work_query.ensure(work_cap)) != BLAZE_OK) return rc;
+        if ((rc = s->out_query.ensure(s->out_cap)) != BLAZE_OK) return rc;
+    }
     const size_t dp_stride = static_cast<size_t>(std::max<uint32_t>(db->max_len, 1)) + 2;
     if ((rc = s->dp.ensure(gapped_warps * 2 * dp_stride)) != BLAZE_OK) return rc;
 
@@ -332,18 +381,12 @@ static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p
     sa.res = db->d_res;
     sa.off = db->d_off;
     sa.n_subj = db->n;
-    sa.q = q->d_q;
-    sa.qlen = q->qlen;
-    sa.cell_start = q->d_cell_start;
-    sa.cell_pack = q->d_cell_pack;
-    sa.presence = q->d_presence;
-    sa.cell_off = q->d_cell_off;
     sa.window = p->window;
     sa.xdrop = p->ungapped_xdrop;
-    sa.cutoff = p->ungapped_cutoff;
     sa.diag_entries = lay.diag_entries;
     sa.diag_magic = lay.diag_magic;
     sa.diag_bytes = lay.diag_bytes;
+    sa.diag_entries_max = lay.diag_entries;
     sa.stage_bytes = lay.stage_bytes;
     sa.query_smem_bytes = lay.query_smem_bytes;
     sa.warp_smem_bytes = lay.warp_smem_bytes;
@@ -352,19 +395,34 @@ static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p
     sa.init_out = s->init_out.p;
     sa.init_cap = s->init_cap;
     sa.work = s->work.p;
-    sa.work_cap = s->work.n;
+    sa.work_cap = work_cap;
     sa.cnt = s->d_cnt;
-    BLAZE_CUDA_TRY(launch_scan(sa, scan_blocks, warps_per_block, lay.smem_bytes, s->stream));
+    if (batched) {
+        sa.queries = s->bq.p;
+        sa.n_queries = r.b->n;
+        sa.tile_subjects = s->tile_subjects;
+        sa.work_query = s->work_query.p;
+        BLAZE_CUDA_TRY(launch_scan_batch(sa, scan_blocks, warps_per_block, lay.smem_bytes, s->stream));
+    } else {
+        const blaze_query *q = r.q;
+        sa.q = q->d_q;
+        sa.qlen = q->qlen;
+        sa.cell_start = q->d_cell_start;
+        sa.cell_pack = q->d_cell_pack;
+        sa.presence = q->d_presence;
+        sa.cell_off = q->d_cell_off;
+        sa.cutoff = p->ungapped_cutoff;
+        sa.n_queries = 1;
+        BLAZE_CUDA_TRY(launch_scan(sa, scan_blocks, warps_per_block, lay.smem_bytes, s->stream));
+    }
     BLAZE_CUDA_TRY(cudaEventRecord(s->ev[2], s->stream));
 
     GappedArgs ga{};
     ga.res = db->d_res;
     ga.off = db->d_off;
-    ga.q = q->d_q;
-    ga.qlen = q->qlen;
     ga.init_in = s->init_out.p;
     ga.work = s->work.p;
-    ga.work_cap = s->work.n;
+    ga.work_cap = work_cap;
     ga.sorted = s->sorted.p;
     ga.saved = s->saved.p;
     ga.cap = s->scratch_cap;
@@ -373,10 +431,20 @@ static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p
     ga.gap_open = p->gap_open;
     ga.gap_extend = p->gap_extend;
     ga.xdrop = p->gapped_xdrop;
-    ga.cutoff = p->gapped_cutoff;
     ga.out = s->out.p;
     ga.out_cap = s->out_cap;
     ga.cnt = s->d_cnt;
+    if (batched) {
+        ga.work_query = s->work_query.p;
+        ga.batch_q = s->bqptr.p;
+        ga.batch_qlen = s->bqlen.p;
+        ga.batch_cutoff = s->bcut.p;
+        ga.out_query = s->out_query.p;
+    } else {
+        ga.q = r.q->d_q;
+        ga.qlen = r.q->qlen;
+        ga.cutoff = p->gapped_cutoff;
+    }
     BLAZE_CUDA_TRY(launch_gapped(ga, s->gapped_blocks, s->stream));
     BLAZE_CUDA_TRY(cudaEventRecord(s->ev[3], s->stream));
     s->stats.kernel_launches += 2;
@@ -386,32 +454,95 @@ static int run_pass(blaze_search *s, const blaze_query *q, const blaze_params *p
     return BLAZE_OK;
 }
 
-extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const blaze_params *p,
-                                uint64_t *n_hsps) {
-    if (!s || !q || q->device != s->db->device) return BLAZE_ERR_INVALID_ARG;
-    int rc = check_params(p);
-    if (rc != BLAZE_OK) return rc;
-    if (p->word_threshold != q->threshold) return BLAZE_ERR_INVALID_ARG;
-    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
+template <typename T>
+static int ensure_pinned(T *&p, size_t &n, size_t want) {
+    if (want <= n) return BLAZE_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    BLAZE_CUDA_TRY(cudaMallocHost(&p, sizeof(T) * want));
+    n = want;
+    return BLAZE_OK;
+}
+
+// Runs both stages (growing buffers and repeating a pass that overflowed),
+// copies the HSPs back and finishes them: E-values, preliminary reap, order
+// by (query, OID).
+static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
+    blaze_db *db = s->db;
+    const blaze_params *p0 = r.p;
+    const bool batched = r.b != nullptr;
+    const uint32_t nq = batched ? r.b->n : 1;
     s->results.clear();
+    s->batch_results.clear();
     s->stats = blaze_stats{};
-    s->stats.h2d_bytes = q->upload_bytes;
     if (n_hsps) *n_hsps = 0;
 
     constexpr size_t kSmemBudget = 220 * 1024;
-    const bool qsmem = q->qlen <= kQuerySmemMax;
-    const ScanLayout lay = scan_layout(q->qlen, p->window, kScanStageBytes, kSmemBudget,
-                                       scan_max_warps_by_registers(qsmem));
+    int32_t max_qlen = 0;
+    for (uint32_t i = 0; i < nq; ++i) max_qlen = std::max(max_qlen, batched ? r.b->qlen[i] : r.q->qlen);
+    const bool qsmem = !batched && max_qlen <= kQuerySmemMax;
+    const int reg_cap = batched ? scan_batch_max_warps_by_registers() : scan_max_warps_by_registers(qsmem);
+    const int warp_cap = s->max_warps ? std::min(reg_cap, static_cast<int>(s->max_warps)) : reg_cap;
+    ScanLayout lay = scan_layout(max_qlen, p0->window, s->stage_bytes, kSmemBudget, warp_cap);
+    if (batched) {
+        // the batched kernel keeps every query in global memory
+        const size_t fixed = kScanMatBytes + kScanPresenceBytes;
+        lay.query_smem_bytes = 0;
+        int w = lay.warps_per_block;
+        while (w < warp_cap && fixed + static_cast<size_t>(w + 1) * lay.warp_smem_bytes <= kSmemBudget) ++w;
+        lay.warps_per_block = w;
+        lay.smem_bytes = fixed + static_cast<size_t>(w) * lay.warp_smem_bytes;
+    }
     if (lay.smem_bytes > 227 * 1024) return BLAZE_ERR_LIMIT;
     int per_sm = 0;
-    BLAZE_CUDA_TRY(scan_occupancy(lay.query_smem_bytes != 0, lay.warps_per_block, lay.smem_bytes, &per_sm));
+    if (batched) {
+        BLAZE_CUDA_TRY(scan_batch_occupancy(lay.warps_per_block, lay.smem_bytes, &per_sm));
+    } else {
+        BLAZE_CUDA_TRY(scan_occupancy(lay.query_smem_bytes != 0, lay.warps_per_block, lay.smem_bytes, &per_sm));
+    }
     if (per_sm < 1) return BLAZE_ERR_LIMIT;
     const int scan_blocks = s->n_sm * per_sm;
 
+    if (batched) {
+        // per-query descriptors of this run (cutoffs come from the parameters)
+        std::vector<BatchQuery> bq(nq);
+        std::vector<const uint8_t *> qp(nq);
+        std::vector<int32_t> ql(nq), cut(nq);
+        for (uint32_t i = 0; i < nq; ++i) {
+            const blaze_params &pi = r.p[i];
+            BatchQuery &d = bq[i];
+            d.q = r.b->d_res + r.b->res_off[i];
+            d.qlen = r.b->qlen[i];
+            d.ungapped_cutoff = pi.ungapped_cutoff;
+            d.cell_start = r.b->d_cell_start + static_cast<size_t>(i) * (kWords + 1);
+            d.cell_pack = r.b->d_cell_pack + static_cast<size_t>(i) * kWords;
+            d.presence = r.b->d_presence + static_cast<size_t>(i) * kPresenceWords;
+            d.cell_off = r.b->d_cell_off + r.b->off_off[i];
+            d.diag_entries = static_cast<uint32_t>(d.qlen + pi.window + 3) & ~3u;
+            d.diag_magic = static_cast<uint32_t>((1ull << 32) / d.diag_entries + 1);
+            qp[i] = d.q;
+            ql[i] = d.qlen;
+            cut[i] = pi.gapped_cutoff;
+        }
+        int rc;
+        if ((rc = s->bq.ensure(nq)) != BLAZE_OK) return rc;
+        if ((rc = s->bqptr.ensure(nq)) != BLAZE_OK) return rc;
+        if ((rc = s->bqlen.ensure(nq)) != BLAZE_OK) return rc;
+        if ((rc = s->bcut.ensure(nq)) != BLAZE_OK) return rc;
+        BLAZE_CUDA_TRY(cudaMemcpyAsync(s->bq.p, bq.data(), sizeof(BatchQuery) * nq, cudaMemcpyHostToDevice, s->stream));
+        BLAZE_CUDA_TRY(cudaMemcpyAsync(s->bqptr.p, qp.data(), sizeof(const uint8_t *) * nq, cudaMemcpyHostToDevice, s->stream));
+        BLAZE_CUDA_TRY(cudaMemcpyAsync(s->bqlen.p, ql.data(), sizeof(int32_t) * nq, cudaMemcpyHostToDevice, s->stream));
+        BLAZE_CUDA_TRY(cudaMemcpyAsync(s->bcut.p, cut.data(), sizeof(int32_t) * nq, cudaMemcpyHostToDevice, s->stream));
+        BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        s->stats.h2d_bytes += (sizeof(BatchQuery) + sizeof(const uint8_t *) + 2 * sizeof(int32_t)) * nq;
+    }
+
     DevCounters c{};
+    int rc;
     BLAZE_CUDA_TRY(cudaEventRecord(s->ev[0], s->stream));
     for (int attempt = 0;; ++attempt) {
-        if ((rc = run_pass(s, q, p, lay, scan_blocks)) != BLAZE_OK) return rc;
+        if ((rc = run_pass(s, r, lay, scan_blocks)) != BLAZE_OK) return rc;
         c = *s->h_cnt;
         {
             float ms = 0.f;
@@ -432,24 +563,27 @@ extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const bla
             s->out_cap = std::max<unsigned long long>(s->out_cap * 2, c.out_count + c.out_count / 4 + 1024);
             again = true;
         }
-        if (c.flags & kFlagWorkArrayFull) return BLAZE_ERR_INTERNAL;  // one item per subject at most
+        if (c.flags & kFlagWorkArrayFull) {
+            if (!batched) return BLAZE_ERR_INTERNAL;  // one item per subject at most
+            s->work_cap = std::max<unsigned long long>(s->work_cap * 2, c.work_count + c.work_count / 4 + 1024);
+            again = true;
+        }
         if (!again) break;
-        if (attempt >= 6) return BLAZE_ERR_INTERNAL;
+        if (attempt >= 8) return BLAZE_ERR_INTERNAL;
         s->stats.reruns++;
     }
 
     // copy back and finish on the host
     const size_t n_out = static_cast<size_t>(c.out_count);
-    if (n_out > s->h_out_n) {
-        if (s->h_out) cudaFreeHost(s->h_out);
-        s->h_out = nullptr;
-        s->h_out_n = 0;
-        BLAZE_CUDA_TRY(cudaMallocHost(&s->h_out, sizeof(DevHsp) * n_out));
-        s->h_out_n = n_out;
-    }
+    if ((rc = ensure_pinned(s->h_out, s->h_out_n, n_out)) != BLAZE_OK) return rc;
+    if (batched && (rc = ensure_pinned(s->h_outq, s->h_outq_n, n_out)) != BLAZE_OK) return rc;
     if (n_out) {
         BLAZE_CUDA_TRY(cudaMemcpyAsync(s->h_out, s->out.p, sizeof(DevHsp) * n_out, cudaMemcpyDeviceToHost, s->stream));
         s->stats.d2h_bytes += sizeof(DevHsp) * n_out;
+        if (batched) {
+            BLAZE_CUDA_TRY(cudaMemcpyAsync(s->h_outq, s->out_query.p, sizeof(uint32_t) * n_out, cudaMemcpyDeviceToHost, s->stream));
+            s->stats.d2h_bytes += sizeof(uint32_t) * n_out;
+        }
     }
     BLAZE_CUDA_TRY(cudaEventRecord(s->ev[3], s->stream));
     BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -460,19 +594,24 @@ extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const bla
         BLAZE_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev[0], s->ev[3]));
         s->stats.device_ms = ms;
     }
-    // groups: each subject's HSPs are contiguous and already in final order
-    struct Group { uint32_t oid; size_t first, n; };
+    // groups: each (query, subject) list is contiguous and already in final order
+    struct Group { uint32_t query, oid; size_t first, n; };
+    auto query_of = [&](size_t i) { return batched ? s->h_outq[i] : 0u; };
     std::vector<Group> groups;
     for (size_t i = 0; i < n_out;) {
         size_t j = i + 1;
-        while (j < n_out && s->h_out[j].subject == s->h_out[i].subject) ++j;
-        groups.push_back({s->db->oid_of[s->h_out[i].subject], i, j - i});
+        while (j < n_out && s->h_out[j].subject == s->h_out[i].subject && query_of(j) == query_of(i)) ++j;
+        groups.push_back({query_of(i), s->db->oid_of[s->h_out[i].subject], i, j - i});
         i = j;
     }
-    std::sort(groups.begin(), groups.end(), [](const Group &a, const Group &b) { return a.oid < b.oid; });
-    s->results.reserve(n_out);
+    std::sort(groups.begin(), groups.end(), [](const Group &a, const Group &b) {
+        return a.query != b.query ? a.query < b.query : a.oid < b.oid;
+    });
+    if (batched) s->batch_results.reserve(n_out);
+    else s->results.reserve(n_out);
     uint32_t subjects = 0;
     for (const Group &g : groups) {
+        const blaze_params &pg = r.p[g.query];
         size_t kept = 0;
         for (size_t k = 0; k < g.n; ++k) {
             const DevHsp &d = s->h_out[g.first + k];
@@ -485,24 +624,91 @@ extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const bla
             h.s_end = d.s_end;
             h.q_gapped_start = d.q_gs;
             h.s_gapped_start = d.s_gs;
-            h.evalue = p->eff_searchsp * p->K * std::exp(-p->lambda * static_cast<double>(d.score));
-            if (h.evalue > p->prelim_evalue) continue;  // preliminary E-value reap
-            s->results.push_back(h);
+            h.evalue = pg.eff_searchsp * pg.K * std::exp(-pg.lambda * static_cast<double>(d.score));
+            if (h.evalue > pg.prelim_evalue) continue;  // preliminary E-value reap
+            if (batched) {
+                blaze_batch_hsp bh;
+                bh.query = g.query;
+                bh.reserved = 0;
+                bh.hsp = h;
+                s->batch_results.push_back(bh);
+            } else {
+                s->results.push_back(h);
+            }
             ++kept;
         }
         subjects += kept > 0;
     }
+    const size_t n_res = batched ? s->batch_results.size() : s->results.size();
     s->last_init_count = c.init_count;
     s->last_work_count = c.work_count;
+    s->last_batched = batched;
     s->stats.residues_scanned = c.residues;
     s->stats.word_hits = c.word_hits;
     s->stats.ungapped_extensions = c.extensions;
     s->stats.init_hsps = c.init_count;
     s->stats.gapped_extensions = c.gapped_ext;
     s->stats.dp_cells = c.dp_cells;
-    s->stats.hsps = s->results.size();
+    s->stats.hsps = n_res;
     s->stats.subjects_with_hsps = subjects;
-    if (n_hsps) *n_hsps = s->results.size();
+    if (n_hsps) *n_hsps = n_res;
+    return BLAZE_OK;
+}
+
+extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const blaze_params *p,
+                                uint64_t *n_hsps) {
+    if (!s || !q || q->device != s->db->device) return BLAZE_ERR_INVALID_ARG;
+    int rc = check_params(p);
+    if (rc != BLAZE_OK) return rc;
+    if (p->word_threshold != q->threshold) return BLAZE_ERR_INVALID_ARG;
+    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
+    RunSpec r;
+    r.q = q;
+    r.p = p;
+    rc = run_search(s, r, n_hsps);
+    s->stats.h2d_bytes += q->upload_bytes;
+    return rc;
+}
+
+extern "C" int blaze_search_run_batch(blaze_search *s, const blaze_batch *b, const blaze_params *params,
+                                      uint64_t *n_hsps) {
+    if (!s || !b || !params || b->device != s->db->device || b->n == 0) return BLAZE_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < b->n; ++i) {
+        int rc = check_params(&params[i]);
+        if (rc != BLAZE_OK) return rc;
+        const blaze_params &a = params[0], &c = params[i];
+        if (c.word_threshold != b->threshold || c.window != a.window || c.ungapped_xdrop != a.ungapped_xdrop ||
+            c.gap_open != a.gap_open || c.gap_extend != a.gap_extend || c.gapped_xdrop != a.gapped_xdrop)
+            return BLAZE_ERR_INVALID_ARG;
+    }
+    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
+    RunSpec r;
+    r.b = b;
+    r.p = params;
+    int rc = run_search(s, r, n_hsps);
+    s->stats.h2d_bytes += b->upload_bytes;
+    return rc;
+}
+
+extern "C" int blaze_search_batch_results(const blaze_search *s, blaze_batch_hsp *out, uint64_t capacity,
+                                          uint64_t *n_hsps) {
+    if (!s) return BLAZE_ERR_INVALID_ARG;
+    if (n_hsps) *n_hsps = s->batch_results.size();
+    if (capacity < s->batch_results.size()) return BLAZE_ERR_OUTPUT_TOO_SMALL;
+    if (!s->batch_results.empty()) {
+        if (!out) return BLAZE_ERR_INVALID_ARG;
+        std::memcpy(out, s->batch_results.data(), sizeof(blaze_batch_hsp) * s->batch_results.size());
+    }
+    return BLAZE_OK;
+}
+
+extern "C" int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t) {
+    if (!s || !t) return BLAZE_ERR_INVALID_ARG;
+    if (t->stage_bytes > 16384 || t->max_warps_per_block > static_cast<uint32_t>(kScanMaxWarpsPerBlock))
+        return BLAZE_ERR_LIMIT;
+    s->stage_bytes = t->stage_bytes ? t->stage_bytes : kScanStageBytes;
+    s->tile_subjects = t->tile_subjects ? t->tile_subjects : kDefaultTileSubjects;
+    s->max_warps = t->max_warps_per_block;
     return BLAZE_OK;
 }
 
@@ -524,9 +730,97 @@ extern "C" int blaze_search_stats(const blaze_search *s, blaze_stats *out) {
     return BLAZE_OK;
 }
 
+extern "C" int blaze_batch_create(const blaze_db *db, const uint8_t *residues, const uint64_t *offsets,
+                                  uint32_t n_queries, int32_t word_threshold, blaze_batch **out) {
+    if (!db || !residues || !offsets || !out || n_queries == 0) return BLAZE_ERR_INVALID_ARG;
+    *out = nullptr;
+    for (uint32_t i = 0; i < n_queries; ++i) {
+        if (offsets[i + 1] <= offsets[i]) return BLAZE_ERR_INVALID_ARG;
+        if (offsets[i + 1] - offsets[i] > static_cast<uint64_t>(kMaxQueryLength)) return BLAZE_ERR_LIMIT;
+        if (!valid_residues(residues + offsets[i], offsets[i + 1] - offsets[i])) return BLAZE_ERR_INVALID_ARG;
+    }
+    BLAZE_CUDA_TRY(cudaSetDevice(db->device));
+    auto *b = new blaze_batch();
+    b->device = db->device;
+    b->n = n_queries;
+    b->threshold = word_threshold;
+    std::vector<uint8_t> res;
+    std::vector<uint32_t> cs_all(static_cast<size_t>(n_queries) * (kWords + 1));
+    std::vector<uint32_t> pack_all(static_cast<size_t>(n_queries) * kWords);
+    std::vector<uint32_t> pres_all(static_cast<size_t>(n_queries) * kPresenceWords, 0u);
+    std::vector<uint16_t> offs_all;
+    for (uint32_t i = 0; i < n_queries; ++i) {
+        const int32_t len = static_cast<int32_t>(offsets[i + 1] - offsets[i]);
+        const uint8_t *q = residues + offsets[i];
+        b->qlen.push_back(len);
+        b->res_off.push_back(res.size());
+        res.insert(res.end(), q, q + len);
+        res.resize((res.size() + 63) & ~static_cast<size_t>(63), 0);  // 64-byte separation
+        uint32_t *cs = cs_all.data() + static_cast<size_t>(i) * (kWords + 1);
+        uint16_t *offs = nullptr;
+        uint32_t n_off = 0;
+        int rc = build_lookup(q, len, word_threshold, cs, &offs, &n_off);
+        if (rc != BLAZE_OK) {
+            delete b;
+            return rc;
+        }
+        b->off_off.push_back(offs_all.size());
+        offs_all.insert(offs_all.end(), offs, offs + n_off);
+        std::free(offs);
+        uint32_t *pk = pack_all.data() + static_cast<size_t>(i) * kWords;
+        uint32_t *pr = pres_all.data() + static_cast<size_t>(i) * kPresenceWords;
+        for (int w = 0; w < kWords; ++w) {
+            const uint32_t cnt = cs[w + 1] - cs[w];
+            pk[w] = (cs[w] << 8) | std::min<uint32_t>(cnt, 255u);
+            if (cnt) pr[w >> 5] |= 1u << (w & 31);
+        }
+    }
+    res.resize(res.size() + 64, 0);
+    if (offs_all.empty()) offs_all.push_back(0);
+    cudaError_t e = cudaMalloc(&b->d_res, res.size());
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_cell_start, sizeof(uint32_t) * cs_all.size());
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_cell_pack, sizeof(uint32_t) * pack_all.size());
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_presence, sizeof(uint32_t) * pres_all.size());
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_cell_off, sizeof(uint16_t) * offs_all.size());
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_res, res.data(), res.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_cell_start, cs_all.data(), sizeof(uint32_t) * cs_all.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_cell_pack, pack_all.data(), sizeof(uint32_t) * pack_all.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_presence, pres_all.data(), sizeof(uint32_t) * pres_all.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_cell_off, offs_all.data(), sizeof(uint16_t) * offs_all.size(), cudaMemcpyHostToDevice);
+    b->upload_bytes = res.size() + sizeof(uint32_t) * (cs_all.size() + pack_all.size() + pres_all.size()) +
+                      sizeof(uint16_t) * offs_all.size();
+    b->device_bytes = b->upload_bytes;
+    if (e != cudaSuccess) {
+        last_cuda_error(e);
+        blaze_batch_free(b);
+        return e == cudaErrorMemoryAllocation ? BLAZE_ERR_OUT_OF_MEMORY : BLAZE_ERR_CUDA;
+    }
+    *out = b;
+    return BLAZE_OK;
+}
+
+extern "C" int blaze_batch_free(blaze_batch *b) {
+    if (!b) return BLAZE_OK;
+    cudaSetDevice(b->device);
+    if (b->d_res) cudaFree(b->d_res);
+    if (b->d_cell_start) cudaFree(b->d_cell_start);
+    if (b->d_cell_pack) cudaFree(b->d_cell_pack);
+    if (b->d_presence) cudaFree(b->d_presence);
+    if (b->d_cell_off) cudaFree(b->d_cell_off);
+    delete b;
+    return BLAZE_OK;
+}
+
+extern "C" int blaze_batch_info(const blaze_batch *b, uint32_t *n_queries, uint64_t *device_bytes) {
+    if (!b) return BLAZE_ERR_INVALID_ARG;
+    if (n_queries) *n_queries = b->n;
+    if (device_bytes) *device_bytes = b->device_bytes;
+    return BLAZE_OK;
+}
+
 extern "C" int blaze_search_init_hits(blaze_search *s, blaze_init_hit *out, uint64_t capacity,
                                       uint64_t *n_hits) {
-    if (!s) return BLAZE_ERR_INVALID_ARG;
+    if (!s || s->last_batched) return BLAZE_ERR_INVALID_ARG;  // single-query runs only
     const size_t n_init = static_cast<size_t>(s->last_init_count);
     const size_t n_work = static_cast<size_t>(s->last_work_count);
     if (n_hits) *n_hits = n_init;

@@ -27,6 +27,7 @@ constexpr size_t kScanMatBytes = kAlphabet * kAlphabet;               // int8 ma
 constexpr size_t kScanPresenceBytes = (kPresenceWords * 4 + 15) & ~15; // 2752
 constexpr int32_t kQuerySmemMax = 8192;      // queries up to this length live in shared memory
 constexpr uint32_t kScanStageBytes = 2048;   // subjects up to this length are staged
+constexpr uint32_t kDefaultTileSubjects = 256;  // subjects per (query, subject range) tile of a batch
 
 // An ungapped HSP that reached the ungapped cutoff (NCBI BlastInitHSP analog).
 struct InitHit {
@@ -71,6 +72,16 @@ constexpr unsigned kFlagOutArrayFull = 4u;
 constexpr unsigned kFlagSavedFull = 8u;
 constexpr unsigned kFlagBadState = 16u;
 
+// One query of a batch, as the batched scan kernel reads it.
+struct BatchQuery {
+    const uint8_t *q;
+    int32_t qlen;
+    int32_t ungapped_cutoff;
+    const uint32_t *cell_start, *cell_pack, *presence;
+    const uint16_t *cell_off;
+    uint32_t diag_entries, diag_magic;
+};
+
 struct ScanArgs {
     const uint8_t *res;        // residues, length-sorted subjects
     const uint64_t *off;       // n_subj + 1 offsets
@@ -85,6 +96,12 @@ struct ScanArgs {
     uint32_t diag_entries;       // >= qlen + window
     uint32_t diag_magic;         // floor(2^32 / diag_entries) + 1
     uint32_t diag_bytes, stage_bytes, query_smem_bytes, warp_smem_bytes;
+    uint32_t diag_entries_max;   // largest table any query of the launch uses
+    // batched launches only
+    const BatchQuery *queries;   // n_queries descriptors
+    uint32_t n_queries;
+    uint32_t tile_subjects;
+    uint32_t *work_query;        // query index of each work item (nullptr: one query)
     InitHit *scratch;          // per warp: scratch_cap records
     uint32_t scratch_cap;
     InitHit *init_out;
@@ -99,6 +116,12 @@ struct GappedArgs {
     const uint64_t *off;
     const uint8_t *q;
     int32_t qlen;
+    // batched launches only: query of each work item and per-query data
+    const uint32_t *work_query;
+    const uint8_t *const *batch_q;
+    const int32_t *batch_qlen;
+    const int32_t *batch_cutoff;
+    uint32_t *out_query;         // query index of each output HSP
     const InitHit *init_in;
     const WorkItem *work;
     unsigned long long work_cap;
@@ -126,6 +149,9 @@ cudaError_t launch_scan(const ScanArgs &a, int n_blocks, int warps_per_block, si
 cudaError_t scan_occupancy(bool query_in_smem, int warps_per_block, size_t smem, int *blocks_per_sm);
 int scan_max_warps_by_registers(bool query_in_smem);
 cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st);
+cudaError_t launch_scan_batch(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem, cudaStream_t st);
+cudaError_t scan_batch_occupancy(int warps_per_block, size_t smem, int *blocks_per_sm);
+int scan_batch_max_warps_by_registers();
 cudaError_t gapped_occupancy(int *blocks_per_sm);
 
 // Host helpers (host.cpp).

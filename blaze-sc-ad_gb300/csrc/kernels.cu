@@ -257,6 +257,10 @@ gapped_kernel(const GappedArgs a) {
         t = __shfl_sync(kFull, t, 0);
         if (t >= n_work) break;
         const WorkItem wi = a.work[t];
+        const uint32_t qi = a.work_query ? a.work_query[t] : 0u;
+        const uint8_t *qres = a.work_query ? a.batch_q[qi] : a.q;
+        const int32_t qlen = a.work_query ? a.batch_qlen[qi] : a.qlen;
+        const int32_t cutoff = a.work_query ? a.batch_cutoff[qi] : a.cutoff;
         const uint32_t n = wi.n_init;
         const InitHit *in = a.init_in + wi.first;
         const uint64_t o0 = a.off[wi.subject];
@@ -285,18 +289,18 @@ gapped_kernel(const GappedArgs a) {
             }
             if (__any_sync(kFull, inside)) continue;
             int32_t q_off = 0;
-            if (lane == 0) q_off = gapped_start(a.q, sub, u.q_start, u.s_start, u.len, mat);
+            if (lane == 0) q_off = gapped_start(qres, sub, u.q_start, u.s_start, u.len, mat);
             q_off = __shfl_sync(kFull, q_off, 0);
             const int32_t s_off = q_off + (u.s_start - u.q_start);
             int32_t al, bl, ar = 0, br = 0, right = 0;
-            const int32_t left = xdrop_dp<true>(a.q, sub, q_off + 1, s_off + 1, a.gap_open, a.gap_extend,
+            const int32_t left = xdrop_dp<true>(qres, sub, q_off + 1, s_off + 1, a.gap_open, a.gap_extend,
                                                 a.xdrop, mat, Hb, Eb, &al, &bl, &cells);
-            if (q_off < a.qlen - 1 && s_off < slen - 1)
-                right = xdrop_dp<false>(a.q + q_off, sub + s_off, a.qlen - q_off - 1, slen - s_off - 1,
+            if (q_off < qlen - 1 && s_off < slen - 1)
+                right = xdrop_dp<false>(qres + q_off, sub + s_off, qlen - q_off - 1, slen - s_off - 1,
                                         a.gap_open, a.gap_extend, a.xdrop, mat, Hb, Eb, &ar, &br, &cells);
             ++n_ext;
             const int32_t score = left + right;
-            if (score >= a.cutoff) {
+            if (score >= cutoff) {
                 if (lane == 0) {
                     DevHsp g;
                     g.subject = wi.subject;
@@ -324,7 +328,10 @@ gapped_kernel(const GappedArgs a) {
             if (base + m > a.out_cap) {
                 if (lane == 0) atomicOr(&a.cnt->flags, kFlagOutArrayFull);
             } else {
-                for (int i = lane; i < m; i += 32) a.out[base + i] = saved[i];
+                for (int i = lane; i < m; i += 32) {
+                    a.out[base + i] = saved[i];
+                    if (a.out_query) a.out_query[base + i] = qi;
+                }
             }
         }
     }

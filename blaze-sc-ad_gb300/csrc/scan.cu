@@ -175,6 +175,17 @@ struct Finder {
     unsigned long long extensions;
 };
 
+// Per-query parameters of the word finder (one query, or the query of the
+// current tile in a batch).
+struct Ctx {
+    const uint8_t *q;
+    int32_t qlen;
+    const uint32_t *cell_start, *cell_pack, *presence;
+    const uint16_t *cell_off;
+    uint32_t diag_entries, diag_magic;
+    int32_t window, xdrop, cutoff;
+};
+
 __device__ __forceinline__ void put_defer(const Finder &f, int buf, int i, int32_t s, int32_t q) {
     reinterpret_cast<uint2 *>(smem)[(f.defer >> 3) + buf * kDeferCap + i] =
         make_uint2(static_cast<uint32_t>(s), static_cast<uint32_t>(q));
@@ -192,30 +203,30 @@ __device__ __forceinline__ int4 get_seed(const Finder &f, int i) {
 // Runs up to 32 hits (one per lane, lanes in hit order) through the two-hit
 // logic. Hits on the same diagonal are taken in lane order; a hit whose
 // diagonal waits on an extension is appended to the deferred list.
-__device__ __forceinline__ void process_batch(Finder &f, const ScanArgs &a, bool valid, int32_t s,
+__device__ __forceinline__ void process_batch(Finder &f, const Ctx &c, bool valid, int32_t s,
                                               int32_t q) {
     if (__ballot_sync(kFull, valid) == 0) return;
-    const uint32_t d = fast_mod(static_cast<uint32_t>(s - q + a.qlen), a.diag_entries, a.diag_magic);
+    const uint32_t d = fast_mod(static_cast<uint32_t>(s - q + c.qlen), c.diag_entries, c.diag_magic);
     const uint32_t doff = f.diag + 4u * d;
     const unsigned lt = lanemask_lt();
     const unsigned peers = __match_any_sync(kFull, valid ? d : 0xffffffffu);
     const unsigned rank = valid ? __popc(peers & lt) : 0u;
     const unsigned max_rank = __reduce_max_sync(kFull, rank);
-    const uint32_t here = static_cast<uint32_t>(s + a.window) + f.base;  // s, biased
+    const uint32_t here = static_cast<uint32_t>(s + c.window) + f.base;  // s, biased
     for (unsigned r = 0; r <= max_rank; ++r) {
         const bool mine = valid && rank == r;
         const uint32_t e = mine ? lds32(doff) : 0u;
         const bool pend = (e & kPendBit) != 0u;
         const bool flag = (e & kFlagBit) != 0u;
-        const int32_t last = static_cast<int32_t>(e & kValMask) - a.window - static_cast<int32_t>(f.base);
+        const int32_t last = static_cast<int32_t>(e & kValMask) - c.window - static_cast<int32_t>(f.base);
         const int32_t diff = s - last;
         // flag set: hits inside the last extension are skipped, the first one
         // past it starts over; otherwise a hit far from the last one starts
         // over, one at distance [wordsize, window) triggers an extension, and
         // an overlapping one is ignored
         const bool defer = mine && pend;
-        const bool seed = mine && !pend && !flag && diff >= kWordSize && diff < a.window;
-        const bool set = mine && !pend && (flag ? s >= last : diff >= a.window);
+        const bool seed = mine && !pend && !flag && diff >= kWordSize && diff < c.window;
+        const bool set = mine && !pend && (flag ? s >= last : diff >= c.window);
         if (set) sts32(doff, here);
         const unsigned dm = __ballot_sync(kFull, defer);
         const unsigned sm = __ballot_sync(kFull, seed);
@@ -238,23 +249,24 @@ __device__ __forceinline__ void process_batch(Finder &f, const ScanArgs &a, bool
 // until no seed and no deferred hit is left. Each replay is shorter than the
 // list it replays whenever it queues a seed, so the loop ends.
 template <bool QS, bool ST>
-__device__ void flush(Finder &f, const ScanArgs &a, const Query<QS> &q, const Subject<ST> &sub) {
+__device__ void flush(Finder &f, const ScanArgs &a, const Ctx &c, const Query<QS> &q,
+                      const Subject<ST> &sub) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
     while (f.n_seed > 0 || f.n_defer > 0) {
-        for (int c = 0; c < f.n_seed; c += 32) {
-            const int i = c + lane;
+        for (int c0 = 0; c0 < f.n_seed; c0 += 32) {
+            const int i = c0 + lane;
             bool pass = false;
             int32_t hq = 0, hs = 0, hl = 0, score = 0;
             int4 sd = make_int4(0, 0, 0, 0);
             if (i < f.n_seed) {
                 sd = get_seed(f, i);
                 int32_t rext, slast;
-                score = extend_two_hit(q, sub, sd.z, sd.y, sd.x, a.xdrop, &hq, &hs, &hl, &rext, &slast);
+                score = extend_two_hit(q, sub, sd.z, sd.y, sd.x, c.xdrop, &hq, &hs, &hl, &rext, &slast);
                 sts32(f.diag + 4u * static_cast<uint32_t>(sd.w),
-                      rext ? (kFlagBit | (static_cast<uint32_t>(slast - (kWordSize - 1) + a.window) + f.base))
-                           : (static_cast<uint32_t>(sd.y + a.window) + f.base));
-                pass = score >= a.cutoff;
+                      rext ? (kFlagBit | (static_cast<uint32_t>(slast - (kWordSize - 1) + c.window) + f.base))
+                           : (static_cast<uint32_t>(sd.y + c.window) + f.base));
+                pass = score >= c.cutoff;
             }
             const unsigned pm = __ballot_sync(kFull, pass);
             if (pass) {
@@ -279,11 +291,11 @@ __device__ void flush(Finder &f, const ScanArgs &a, const Query<QS> &q, const Su
             const int old = f.sel, n_old = f.n_defer;
             f.sel ^= 1;
             f.n_defer = 0;
-            for (int c = 0; c < n_old; c += 32) {
-                const int i = c + lane;
+            for (int c0 = 0; c0 < n_old; c0 += 32) {
+                const int i = c0 + lane;
                 const bool v = i < n_old;
                 const uint2 h = v ? get_defer(f, old, i) : make_uint2(0u, 0u);
-                process_batch(f, a, v, static_cast<int32_t>(h.x), static_cast<int32_t>(h.y));
+                process_batch(f, c, v, static_cast<int32_t>(h.x), static_cast<int32_t>(h.y));
             }
         }
     }
@@ -292,9 +304,9 @@ __device__ void flush(Finder &f, const ScanArgs &a, const Query<QS> &q, const Su
 // Word scan of one subject: chunks of 128 positions, four consecutive
 // positions per lane; one warp prefix sum per chunk lays the hits out in
 // (subject offset, query offset) order, and lanes take them 32 at a time.
-template <bool QS, bool ST>
-__device__ __forceinline__ unsigned long long scan_subject(Finder &f, const ScanArgs &a, const Query<QS> &q,
-                                                           const Subject<ST> &sub) {
+template <bool QS, bool ST, bool PSMEM>
+__device__ __forceinline__ unsigned long long scan_subject(Finder &f, const ScanArgs &a, const Ctx &c,
+                                                           const Query<QS> &q, const Subject<ST> &sub) {
     const int lane = threadIdx.x & 31;
     unsigned long long word_hits = 0;
     const int32_t nwords = sub.len - (kWordSize - 1);
@@ -307,11 +319,12 @@ __device__ __forceinline__ unsigned long long scan_subject(Finder &f, const Scan
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const uint32_t w = r[j] * 784u + r[j + 1] * 28u + r[j + 2];
-            const bool present = p0 + j < nwords && ((lds32(kPresOff + 4u * (w >> 5)) >> (w & 31u)) & 1u);
-            const uint32_t pk = present ? __ldg(a.cell_pack + w) : 0u;
+            const uint32_t pw = PSMEM ? lds32(kPresOff + 4u * (w >> 5)) : __ldg(c.presence + (w >> 5));
+            const bool present = p0 + j < nwords && ((pw >> (w & 31u)) & 1u);
+            const uint32_t pk = present ? __ldg(c.cell_pack + w) : 0u;
             cs[j] = pk >> 8;
             cnt[j] = pk & 0xffu;
-            if (cnt[j] == 0xffu) cnt[j] = __ldg(a.cell_start + w + 1) - cs[j];
+            if (cnt[j] == 0xffu) cnt[j] = __ldg(c.cell_start + w + 1) - cs[j];
         }
         const uint32_t mine_total = cnt[0] + cnt[1] + cnt[2] + cnt[3];
         uint32_t incl = mine_total;
@@ -342,117 +355,199 @@ __device__ __forceinline__ unsigned long long scan_subject(Finder &f, const Scan
             const uint32_t Ej = j == 0 ? E0 : j == 1 ? E1 : j == 2 ? E2 : E3;
             const uint32_t Cj = j == 0 ? C0 : j == 1 ? C1 : j == 2 ? C2 : C3;
             const bool hv = k < total;
-            const int32_t qo = hv ? static_cast<int32_t>(__ldg(a.cell_off + Cj + (k - Ej))) : 0;
-            process_batch(f, a, hv, cb + 4 * lo + j, qo);
-            if (f.n_seed >= 32 || f.n_defer > kDeferCap - 32) flush(f, a, q, sub);
+            const int32_t qo = hv ? static_cast<int32_t>(__ldg(c.cell_off + Cj + (k - Ej))) : 0;
+            process_batch(f, c, hv, cb + 4 * lo + j, qo);
+            if (f.n_seed >= 32 || f.n_defer > kDeferCap - 32) flush(f, a, c, q, sub);
         }
     }
-    flush(f, a, q, sub);
+    flush(f, a, c, q, sub);
     return word_hits;
 }
 
-template <bool QS>
-__global__ void __launch_bounds__(kScanMaxWarpsPerBlock * 32, 1)
-scan_kernel(const ScanArgs a) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < kAlphabet * kAlphabet; i += blockDim.x)
-        reinterpret_cast<int8_t *>(smem)[kMatOff + i] = g_blosum8[i];
-    for (int i = threadIdx.x; i < kPresenceWords; i += blockDim.x) sts32(kPresOff + 4u * i, a.presence[i]);
-    if (QS)
-        for (int i = threadIdx.x; i < a.qlen; i += blockDim.x) smem[kQueryOff + i] = a.q[i];
+// One subject for the query of `c`: stage it when it fits, find its init
+// hits, and publish them as one contiguous block with a work item.
+template <bool QS, bool PSMEM>
+__device__ __forceinline__ void process_subject(Finder &f, const ScanArgs &a, const Ctx &c, const Query<QS> &q,
+                                                uint32_t subj, uint32_t query_index, uint32_t stage,
+                                                unsigned long long &word_hits, unsigned long long &residues) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t o0 = a.off[subj];
+    const int32_t slen = static_cast<int32_t>(a.off[subj + 1] - o0);
+    f.n_init = 0;
+    residues += static_cast<unsigned long long>(slen);
+    if (static_cast<uint32_t>(slen) <= a.stage_bytes) {
+        // stage the subject: 16-byte aligned vectors covering it (the
+        // database is padded, so the last vector stays in bounds)
+        const uint32_t lead = static_cast<uint32_t>(o0 & 15u);
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.res + (o0 - lead));
+        const uint32_t nvec = (lead + static_cast<uint32_t>(slen) + 15u) >> 4;
+        for (uint32_t i = lane; i < nvec; i += 32) reinterpret_cast<uint4 *>(smem)[(stage >> 4) + i] = __ldg(src + i);
+        __syncwarp();
+        Subject<true> sub;
+        sub.off = stage + lead;
+        sub.ptr = nullptr;
+        sub.len = slen;
+        word_hits += scan_subject<QS, true, PSMEM>(f, a, c, q, sub);
+    } else {
+        Subject<false> sub;
+        sub.off = 0;
+        sub.ptr = a.res + o0;
+        sub.len = slen;
+        word_hits += scan_subject<QS, false, PSMEM>(f, a, c, q, sub);
+    }
 
-    const uint32_t mine = kQueryOff + a.query_smem_bytes + static_cast<uint32_t>(warp) * a.warp_smem_bytes;
+    // publish this subject's init hits as one contiguous block
+    if (f.n_init > 0) {
+        if (f.n_init > a.scratch_cap) {
+            if (lane == 0) {
+                atomicAdd(&a.cnt->overflow_subjects, 1u);
+                atomicMax(&a.cnt->max_init_needed, f.n_init);
+            }
+        } else {
+            unsigned long long first = 0, wi = 0;
+            if (lane == 0) {
+                first = atomicAdd(&a.cnt->init_count, static_cast<unsigned long long>(f.n_init));
+                wi = atomicAdd(&a.cnt->work_count, 1ull);
+            }
+            first = __shfl_sync(kFull, first, 0);
+            wi = __shfl_sync(kFull, wi, 0);
+            if (first + f.n_init > a.init_cap || wi >= a.work_cap) {
+                if (lane == 0)
+                    atomicOr(&a.cnt->flags, first + f.n_init > a.init_cap ? kFlagInitArrayFull : kFlagWorkArrayFull);
+            } else {
+                for (uint32_t i = lane; i < f.n_init; i += 32) a.init_out[first + i] = f.scratch[i];
+                if (lane == 0) {
+                    WorkItem w;
+                    w.subject = subj;
+                    w.n_init = f.n_init;
+                    w.first = first;
+                    a.work[wi] = w;
+                    if (a.work_query) a.work_query[wi] = query_index;
+                }
+            }
+        }
+    }
+    f.base += static_cast<uint32_t>(slen + c.window);
+    __syncwarp();
+    if (f.base > kBaseReset) {
+        for (uint32_t i = lane; i < a.diag_entries_max; i += 32) sts32(f.diag + 4u * i, 0u);
+        f.base = 0;
+        __syncwarp();
+    }
+}
+
+__device__ __forceinline__ Finder make_finder(const ScanArgs &a, uint32_t qbytes, uint32_t &stage) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t mine = kQueryOff + qbytes + static_cast<uint32_t>(warp) * a.warp_smem_bytes;
     Finder f;
     f.diag = mine;
     f.defer = mine + a.diag_bytes;
     f.seeds = f.defer + 2u * kDeferCap * sizeof(uint2);
-    const uint32_t stage = f.seeds + kSeedCap * sizeof(int4);
+    stage = f.seeds + kSeedCap * sizeof(int4);
     f.n_defer = f.n_seed = f.sel = 0;
     f.base = 0;
     f.extensions = 0;
     const unsigned long long gwarp = (static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     f.scratch = a.scratch + gwarp * a.scratch_cap;
-    for (uint32_t i = lane; i < a.diag_entries; i += 32) sts32(f.diag + 4u * i, 0u);
+    for (uint32_t i = lane; i < a.diag_entries_max; i += 32) sts32(f.diag + 4u * i, 0u);
+    return f;
+}
+
+__device__ __forceinline__ void finish_counters(const ScanArgs &a, const Finder &f, unsigned long long word_hits,
+                                                unsigned long long residues) {
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&a.cnt->word_hits, word_hits);
+        atomicAdd(&a.cnt->residues, residues);
+        atomicAdd(&a.cnt->extensions, f.extensions);
+    }
+}
+
+// One query against the whole database: the query's presence bitset (and
+// the query itself when short enough) live in shared memory; warps pull
+// subjects longest first.
+template <bool QS>
+__global__ void __launch_bounds__(kScanMaxWarpsPerBlock * 32, 1)
+scan_kernel(const ScanArgs a) {
+    const int lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < kAlphabet * kAlphabet; i += blockDim.x)
+        reinterpret_cast<int8_t *>(smem)[kMatOff + i] = g_blosum8[i];
+    for (int i = threadIdx.x; i < kPresenceWords; i += blockDim.x) sts32(kPresOff + 4u * i, a.presence[i]);
+    if (QS)
+        for (int i = threadIdx.x; i < a.qlen; i += blockDim.x) smem[kQueryOff + i] = a.q[i];
+    uint32_t stage = 0;
+    Finder f = make_finder(a, a.query_smem_bytes, stage);
     __syncthreads();
+    Ctx c;
+    c.q = a.q;
+    c.qlen = a.qlen;
+    c.cell_start = a.cell_start;
+    c.cell_pack = a.cell_pack;
+    c.presence = a.presence;
+    c.cell_off = a.cell_off;
+    c.diag_entries = a.diag_entries;
+    c.diag_magic = a.diag_magic;
+    c.window = a.window;
+    c.xdrop = a.xdrop;
+    c.cutoff = a.cutoff;
     Query<QS> q;
     q.ptr = a.q;
     q.len = a.qlen;
-
     unsigned long long word_hits = 0, residues = 0;
     for (;;) {
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(&a.cnt->next_scan, 1ull);
         t = __shfl_sync(kFull, t, 0);
         if (t >= a.n_subj) break;
-        const uint32_t subj = a.n_subj - 1 - static_cast<uint32_t>(t);
-        const uint64_t o0 = a.off[subj];
-        const int32_t slen = static_cast<int32_t>(a.off[subj + 1] - o0);
-        f.n_init = 0;
-        residues += static_cast<unsigned long long>(slen);
-        if (static_cast<uint32_t>(slen) <= a.stage_bytes) {
-            // stage the subject: 16-byte aligned vectors covering it (the
-            // database is padded, so the last vector stays in bounds)
-            const uint32_t lead = static_cast<uint32_t>(o0 & 15u);
-            const uint4 *src = reinterpret_cast<const uint4 *>(a.res + (o0 - lead));
-            const uint32_t nvec = (lead + static_cast<uint32_t>(slen) + 15u) >> 4;
-            for (uint32_t i = lane; i < nvec; i += 32) reinterpret_cast<uint4 *>(smem)[(stage >> 4) + i] = __ldg(src + i);
-            __syncwarp();
-            Subject<true> sub;
-            sub.off = stage + lead;
-            sub.ptr = nullptr;
-            sub.len = slen;
-            word_hits += scan_subject(f, a, q, sub);
-        } else {
-            Subject<false> sub;
-            sub.off = 0;
-            sub.ptr = a.res + o0;
-            sub.len = slen;
-            word_hits += scan_subject(f, a, q, sub);
-        }
+        process_subject<QS, true>(f, a, c, q, a.n_subj - 1 - static_cast<uint32_t>(t), 0u, stage, word_hits, residues);
+    }
+    finish_counters(a, f, word_hits, residues);
+}
 
-        // publish this subject's init hits as one contiguous block
-        if (f.n_init > 0) {
-            if (f.n_init > a.scratch_cap) {
-                if (lane == 0) {
-                    atomicAdd(&a.cnt->overflow_subjects, 1u);
-                    atomicMax(&a.cnt->max_init_needed, f.n_init);
-                }
-            } else {
-                unsigned long long first = 0, wi = 0;
-                if (lane == 0) {
-                    first = atomicAdd(&a.cnt->init_count, static_cast<unsigned long long>(f.n_init));
-                    wi = atomicAdd(&a.cnt->work_count, 1ull);
-                }
-                first = __shfl_sync(kFull, first, 0);
-                wi = __shfl_sync(kFull, wi, 0);
-                if (first + f.n_init > a.init_cap || wi >= a.work_cap) {
-                    if (lane == 0)
-                        atomicOr(&a.cnt->flags, first + f.n_init > a.init_cap ? kFlagInitArrayFull : kFlagWorkArrayFull);
-                } else {
-                    for (uint32_t i = lane; i < f.n_init; i += 32) a.init_out[first + i] = f.scratch[i];
-                    if (lane == 0) {
-                        WorkItem w;
-                        w.subject = subj;
-                        w.n_init = f.n_init;
-                        w.first = first;
-                        a.work[wi] = w;
-                    }
-                }
-            }
-        }
-        f.base += static_cast<uint32_t>(slen + a.window);
-        __syncwarp();
-        if (f.base > kBaseReset) {
-            for (uint32_t i = lane; i < a.diag_entries; i += 32) sts32(f.diag + 4u * i, 0u);
-            f.base = 0;
-            __syncwarp();
-        }
+// Many queries against the database: warps pull (query, subject range)
+// tiles; tile t covers query t mod n_queries and the (t / n_queries)-th
+// range counted from the longest subjects down, so every query's long
+// subjects come first and queries interleave. Query tables stay in global
+// memory (L1/L2 resident).
+__global__ void __launch_bounds__(kScanMaxWarpsPerBlock * 32, 1)
+scan_batch_kernel(const ScanArgs a) {
+    const int lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < kAlphabet * kAlphabet; i += blockDim.x)
+        reinterpret_cast<int8_t *>(smem)[kMatOff + i] = g_blosum8[i];
+    uint32_t stage = 0;
+    Finder f = make_finder(a, 0u, stage);
+    __syncthreads();
+    const uint32_t ranges = (a.n_subj + a.tile_subjects - 1) / a.tile_subjects;
+    const unsigned long long n_tiles = static_cast<unsigned long long>(ranges) * a.n_queries;
+    unsigned long long word_hits = 0, residues = 0;
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(&a.cnt->next_scan, 1ull);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= n_tiles) break;
+        const uint32_t qi = static_cast<uint32_t>(t % a.n_queries);
+        const uint32_t range = static_cast<uint32_t>(t / a.n_queries);
+        const BatchQuery bq = a.queries[qi];
+        Ctx c;
+        c.q = bq.q;
+        c.qlen = bq.qlen;
+        c.cell_start = bq.cell_start;
+        c.cell_pack = bq.cell_pack;
+        c.presence = bq.presence;
+        c.cell_off = bq.cell_off;
+        c.diag_entries = bq.diag_entries;
+        c.diag_magic = bq.diag_magic;
+        c.window = a.window;
+        c.xdrop = a.xdrop;
+        c.cutoff = bq.ungapped_cutoff;
+        Query<false> q;
+        q.ptr = bq.q;
+        q.len = bq.qlen;
+        const uint32_t hi = a.n_subj - range * a.tile_subjects;  // exclusive, counted from the end
+        const uint32_t lo = hi > a.tile_subjects ? hi - a.tile_subjects : 0u;
+        for (uint32_t subj = hi; subj-- > lo;)
+            process_subject<false, false>(f, a, c, q, subj, qi, stage, word_hits, residues);
     }
-    if (lane == 0) {
-        atomicAdd(&a.cnt->word_hits, word_hits);
-        atomicAdd(&a.cnt->residues, residues);
-        atomicAdd(&a.cnt->extensions, f.extensions);
-    }
+    finish_counters(a, f, word_hits, residues);
 }
 
 }  // namespace
@@ -491,6 +586,33 @@ int scan_max_warps_by_registers(bool query_in_smem) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&regs_per_block, cudaDevAttrMaxRegistersPerBlock, dev);
     // registers are granted per warp in blocks of 256
+    const int per_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
+    return per_warp > 0 ? std::max(1, std::min(kScanMaxWarpsPerBlock, std::min(fa.maxThreadsPerBlock / 32, regs_per_block / per_warp))) : kScanMaxWarpsPerBlock;
+}
+
+cudaError_t launch_scan_batch(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem_bytes,
+                              cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(scan_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem_bytes));
+    if (e != cudaSuccess) return e;
+    scan_batch_kernel<<<n_blocks, warps_per_block * 32, smem_bytes, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t scan_batch_occupancy(int warps_per_block, size_t smem_bytes, int *blocks_per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(scan_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem_bytes));
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, scan_batch_kernel, warps_per_block * 32,
+                                                         smem_bytes);
+}
+
+int scan_batch_max_warps_by_registers() {
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, scan_batch_kernel) != cudaSuccess) return kScanMaxWarpsPerBlock;
+    int dev = 0, regs_per_block = 65536;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&regs_per_block, cudaDevAttrMaxRegistersPerBlock, dev);
     const int per_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
     return per_warp > 0 ? std::max(1, std::min(kScanMaxWarpsPerBlock, std::min(fa.maxThreadsPerBlock / 32, regs_per_block / per_warp))) : kScanMaxWarpsPerBlock;
 }

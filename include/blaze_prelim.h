@@ -153,11 +153,54 @@ int blaze_search_results(const blaze_search *s, blaze_hsp *out, uint64_t capacit
                          uint64_t *n_hsps);
 int blaze_search_stats(const blaze_search *s, blaze_stats *out);
 
-/* Diagnostics: the init hits of the last run, grouped by OID (ascending) and
+/* Diagnostics: the init hits of the last single-query run, grouped by OID (ascending) and
  * in the order the gapped stage visits them (score descending, then subject
  * and query offset of the trigger). Same capacity rule as above. */
 int blaze_search_init_hits(blaze_search *s, blaze_init_hit *out, uint64_t capacity,
                            uint64_t *n_hits);
+
+/* ---------------------------------------------------------------------
+ * Batched form: many queries of uneven length against the database in one
+ * persistent launch per stage. Warps pull (query, subject range) tiles from a
+ * device work queue, longest subjects first, queries interleaved. All
+ * queries of a batch share word_threshold, window, X-drops and gap costs;
+ * cutoffs and E-value statistics are per query (params[i]).
+ */
+typedef struct blaze_batch blaze_batch;
+
+/* One HSP of a batched run: the query's index in the batch and the HSP. */
+typedef struct blaze_batch_hsp {
+    uint32_t query;
+    uint32_t reserved;
+    blaze_hsp hsp;
+} blaze_batch_hsp;
+
+/* Queries residues[offsets[i] .. offsets[i+1]), i < n_queries, each valid as
+ * for blaze_query_create. */
+int blaze_batch_create(const blaze_db *db, const uint8_t *residues, const uint64_t *offsets,
+                       uint32_t n_queries, int32_t word_threshold, blaze_batch **out);
+int blaze_batch_free(blaze_batch *b);
+/* Device memory the batch's tables take (the serving loop admits by it). */
+int blaze_batch_info(const blaze_batch *b, uint32_t *n_queries, uint64_t *device_bytes);
+
+/* Runs every query of b; params points to n_queries parameter sets. Results
+ * are held by s until the next run. */
+int blaze_search_run_batch(blaze_search *s, const blaze_batch *b, const blaze_params *params,
+                           uint64_t *n_hsps);
+/* Results of the last batched run, grouped by query, then OID (ascending),
+ * then NCBI's per-subject order. Same capacity rule as blaze_search_results. */
+int blaze_search_batch_results(const blaze_search *s, blaze_batch_hsp *out, uint64_t capacity,
+                               uint64_t *n_hsps);
+
+/* Launch shape of the word finder (0 = library default): subjects up to
+ * stage_bytes residues are staged in shared memory; a batched tile covers
+ * tile_subjects subjects; max_warps_per_block caps the block. */
+typedef struct blaze_tuning {
+    uint32_t stage_bytes;
+    uint32_t tile_subjects;
+    uint32_t max_warps_per_block;
+} blaze_tuning;
+int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t);
 
 /* Convenience: blaze_query_create + blaze_search_run + blaze_search_results
  * in one call with host buffers (the drop-in path). */

@@ -1,0 +1,107 @@
+"""GPU tests of the batched form: many queries in one launch per stage must
+give, query by query, exactly the HSP lists of the plain one-query path (and
+of the oracle), whatever the tile size, staging size and block shape."""
+import numpy as np
+import pytest
+
+import blaze103
+from blaze103 import synth
+
+from _parity import concat, oracle_run, params_for
+
+pytestmark = pytest.mark.gpu
+
+
+def _db(seed=21, n=3000, with_homologs_of=None):
+    rng = np.random.default_rng(seed)
+    seqs = [synth.random_residues(rng, int(L)) for L in synth.lognormal_lengths(rng, n, 250, 0.82, 30, 5000)]
+    for i in range(0, len(seqs), 7):
+        if with_homologs_of:
+            q = with_homologs_of[i % len(with_homologs_of)]
+            w = min(len(q), int(rng.integers(40, 300)))
+            s0 = int(rng.integers(0, len(q) - w + 1))
+            seqs[i] = np.concatenate([seqs[i], synth.mutate(rng, q[s0:s0 + w], 0.45)])
+    seqs.sort(key=len)
+    return concat(seqs)
+
+
+def _queries(seed=22, lengths=(5, 50, 120, 300, 333, 700, 1000, 1500, 2600, 9000)):
+    rng = np.random.default_rng(seed)
+    return [synth.random_residues(rng, L) for L in lengths]
+
+
+def _plain(ps, db, q, p):
+    qq = blaze103.Query(db, q)
+    try:
+        ps.run_query(qq, p)
+        return ps.results()
+    finally:
+        qq.close()
+
+
+def _check_batch_equals_plain(tuning=None):
+    qs = _queries()
+    res, off = _db(with_homologs_of=qs)
+    db = blaze103.SeqSrc(res, off)
+    ps = blaze103.PrelimSearch(db)
+    params = [params_for(len(q), db.tot_len, db.num_seqs)[0] for q in qs]
+    want = [_plain(ps, db, q, p) for q, p in zip(qs, params)]
+    if tuning:
+        ps.set_tuning(**tuning)
+    batch = blaze103.QueryBatch(db, qs)
+    got = ps.run_batch(batch, params)
+    assert np.all(np.diff(got["query"].astype(np.int64)) >= 0)
+    total = 0
+    for i, w in enumerate(want):
+        g = got[got["query"] == i]
+        for f in blaze103.HSP_DTYPE.names:
+            assert np.array_equal(g[f], w[f]), (i, f)
+        total += len(w)
+    assert total == len(got) and total > 50
+    batch.close()
+    ps.close()
+    db.close()
+    return qs, res, off, params, got
+
+
+def test_batch_equals_plain_per_query():
+    qs, res, off, params, got = _check_batch_equals_plain()
+    # and two of the queries against the oracle directly
+    for i in (3, 6):
+        pd = params_for(len(qs[i]), int(off[-1]), len(off) - 1)[1]
+        ref, _ = oracle_run(qs[i], res, off, pd)
+        g = got[got["query"] == i]
+        assert np.array_equal(g["oid"], ref["subject"])
+        for f in ("score", "q_start", "q_end", "s_start", "s_end"):
+            assert np.array_equal(g[f], ref[f]), f
+
+
+@pytest.mark.parametrize("tuning", [dict(tile_subjects=1), dict(tile_subjects=4096),
+                                    dict(stage_bytes=512, max_warps_per_block=3),
+                                    dict(stage_bytes=8192, tile_subjects=33)])
+def test_batch_tuning_does_not_change_results(tuning):
+    _check_batch_equals_plain(tuning)
+
+
+def test_batch_capacity_regrowth(monkeypatch):
+    monkeypatch.setenv("BLAZE_INITIAL_SCRATCH_CAP", "2")
+    monkeypatch.setenv("BLAZE_INITIAL_INIT_CAP", "5")
+    monkeypatch.setenv("BLAZE_INITIAL_OUT_CAP", "5")
+    monkeypatch.setenv("BLAZE_INITIAL_WORK_CAP", "3")
+    _check_batch_equals_plain()
+
+
+def test_batch_rejects_mixed_search_settings():
+    qs = _queries(lengths=(100, 200))
+    res, off = _db(n=200)
+    db = blaze103.SeqSrc(res, off)
+    ps = blaze103.PrelimSearch(db)
+    p = [params_for(len(q), db.tot_len, db.num_seqs)[0] for q in qs]
+    p[1].window = 30
+    batch = blaze103.QueryBatch(db, qs)
+    with pytest.raises(blaze103.BlazeError) as e:
+        ps.run_batch(batch, p)
+    assert e.value.status == 1
+    batch.close()
+    ps.close()
+    db.close()
