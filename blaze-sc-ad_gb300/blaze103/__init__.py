@@ -24,10 +24,10 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import (BATCH_HSP_DTYPE, HSP_DTYPE, INIT_DTYPE, BlazeError, BlazeParams, BlazeStats,
-                   BlazeTuning, check, load, u8ptr, u64ptr, status_string)
+from ._lib import (BATCH_HSP_DTYPE, HSP_DTYPE, INIT_DTYPE, BlazeError, BlazeParams, BlazeServerConfig,
+                   BlazeServerStats, BlazeStats, BlazeTuning, check, load, u8ptr, u64ptr, status_string)
 
-__all__ = ["SeqSrc", "PrelimSearch", "HSPResults", "QueryBatch", "BlazeParams", "BlazeTuning",
+__all__ = ["SeqSrc", "PrelimSearch", "HSPResults", "QueryBatch", "Server", "BlazeParams", "BlazeTuning",
            "BlazeError", "HSP_DTYPE", "BATCH_HSP_DTYPE", "default_params", "device_count", "load",
            "status_string"]
 
@@ -182,9 +182,14 @@ class QueryBatch:
 class PrelimSearch:
     """Runs the preliminary search stage against one SeqSrc (one CUDA stream)."""
 
-    def __init__(self, seq_src: SeqSrc):
+    def __init__(self, seq_src: SeqSrc, autotune: bool = True):
+        """autotune: batched runs take their launch shape from the committed
+        autotuner table (blaze103/tuning.json, nearest shape) until
+        ``set_tuning`` is called."""
         self._lib = load()
         self.seq_src = seq_src
+        self._auto = autotune
+        self._applied = None
         h = ctypes.c_void_p()
         check(self._lib.blaze_search_create(seq_src.handle, ctypes.byref(h)), "blaze_search_create")
         self._h = h
@@ -227,15 +232,34 @@ class PrelimSearch:
         finally:
             q.close()
 
-    def set_tuning(self, stage_bytes: int = 0, tile_subjects: int = 0, max_warps_per_block: int = 0):
-        t = BlazeTuning(int(stage_bytes), int(tile_subjects), int(max_warps_per_block))
+    def set_tuning(self, stage_bytes: int = 0, tile_subjects: int = 0, max_warps_per_block: int = 0,
+                   launch_mode: int = 0):
+        """Launch shape (0 = library default for each); launch_mode 0: CUDA
+        graph for batched runs, 1: direct launches, 2: CUDA graph always."""
+        self._auto = False
+        self._set_tuning(stage_bytes, tile_subjects, max_warps_per_block, launch_mode)
+
+    def _set_tuning(self, stage_bytes=0, tile_subjects=0, max_warps_per_block=0, launch_mode=0):
+        t = BlazeTuning(int(stage_bytes), int(tile_subjects), int(max_warps_per_block), int(launch_mode))
         check(self._lib.blaze_search_set_tuning(self._h, ctypes.byref(t)), "blaze_search_set_tuning")
+
+    @property
+    def tuning(self) -> dict | None:
+        """The autotuned launch shape applied to the last batched run, if any."""
+        return self._applied
 
     def run_batch(self, batch: QueryBatch, params=None, evalue: float = 10.0) -> np.ndarray:
         """Every query of the batch in one batched launch; returns
         BATCH_HSP_DTYPE records grouped by query, then OID."""
         if params is None:
             params = [default_params(L, self.seq_src, evalue) for L in batch.lengths]
+        if self._auto:
+            from .autotune import lookup
+
+            t = lookup("batched", len(batch), float(np.median(batch.lengths)), self.seq_src.tot_len)
+            if t and t != self._applied:
+                self._set_tuning(**t)
+                self._applied = t
         arr = (BlazeParams * len(params))(*params)
         n = ctypes.c_uint64()
         check(self._lib.blaze_search_run_batch(self._h, batch.handle, arr, ctypes.byref(n)),
@@ -259,6 +283,65 @@ class PrelimSearch:
     def close(self) -> None:
         if getattr(self, "_h", None):
             self._lib.blaze_search_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop over a resident database (``blaze_server_*``): queries are
+    submitted as they arrive and run in continuously formed batches, ``slots``
+    batches in flight at once, admitted under ``memory_budget`` device bytes.
+    Each query's result is exactly what ``PrelimSearch.run`` returns for it
+    alone with ``default_params(len(query), seq_src, evalue)``."""
+
+    def __init__(self, seq_src: SeqSrc, slots: int = 2, max_batch: int = 64, memory_budget: int = 0,
+                 batch_window_us: int = 200, evalue: float = 10.0, tuning: dict | None = None):
+        """tuning: launch shape of the workers' searches (BlazeTuning fields);
+        None takes the autotuner's entry for batches of max_batch queries."""
+        self._lib = load()
+        self._src = seq_src
+        if tuning is None:
+            from .autotune import lookup
+
+            tuning = lookup("batched", max_batch, 350.0, seq_src.tot_len) or {}
+        self.tuning = dict(tuning)
+        cfg = BlazeServerConfig(slots, max_batch, memory_budget, batch_window_us, evalue,
+                                BlazeTuning(*(int(tuning.get(k, 0)) for k, _ in BlazeTuning._fields_)))
+        h = ctypes.c_void_p()
+        check(self._lib.blaze_server_create(seq_src.handle, ctypes.byref(cfg), ctypes.byref(h)),
+              "blaze_server_create")
+        self._h = h
+
+    def submit(self, query) -> int:
+        q = _codes(query, "query")
+        t = ctypes.c_uint64()
+        check(self._lib.blaze_server_submit(self._h, u8ptr(q), q.size, ctypes.byref(t)), "blaze_server_submit")
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> np.ndarray:
+        """Blocks until the ticket completed; returns its HSPs (grouped by OID)."""
+        n = ctypes.c_uint64()
+        check(self._lib.blaze_server_wait(self._h, ticket, timeout_ms, ctypes.byref(n)), "blaze_server_wait")
+        out = np.empty(n.value, dtype=HSP_DTYPE)
+        lat = ctypes.c_double()
+        check(self._lib.blaze_server_take(self._h, ticket, out.ctypes.data_as(ctypes.c_void_p), n.value,
+                                          ctypes.byref(n), ctypes.byref(lat)), "blaze_server_take")
+        self.last_latency_ms = lat.value
+        return out[: n.value]
+
+    def stats(self) -> dict:
+        st = BlazeServerStats()
+        check(self._lib.blaze_server_stats_get(self._h, ctypes.byref(st)), "blaze_server_stats_get")
+        return st.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.blaze_server_free(self._h)
             self._h = None
 
     def __del__(self):

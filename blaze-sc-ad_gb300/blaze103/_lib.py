@@ -18,6 +18,8 @@ EXPORTS = (
     "blaze_search_stats", "blaze_search_init_hits", "blaze_prelim_search",
     "blaze_batch_create", "blaze_batch_free", "blaze_batch_info", "blaze_search_run_batch",
     "blaze_search_batch_results", "blaze_search_set_tuning",
+    "blaze_server_create", "blaze_server_submit", "blaze_server_wait", "blaze_server_take",
+    "blaze_server_stats_get", "blaze_server_free",
 )
 
 HSP_DTYPE = np.dtype([
@@ -51,7 +53,7 @@ class BlazeParams(ctypes.Structure):
 
 class BlazeTuning(ctypes.Structure):
     _fields_ = [("stage_bytes", ctypes.c_uint32), ("tile_subjects", ctypes.c_uint32),
-                ("max_warps_per_block", ctypes.c_uint32)]
+                ("max_warps_per_block", ctypes.c_uint32), ("launch_mode", ctypes.c_uint32)]
 
 
 class BlazeStats(ctypes.Structure):
@@ -63,6 +65,25 @@ class BlazeStats(ctypes.Structure):
         ("reruns", ctypes.c_uint32), ("scan_ms", ctypes.c_float), ("gapped_ms", ctypes.c_float),
         ("device_ms", ctypes.c_float), ("kernel_launches", ctypes.c_uint32),
         ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+        ("graph_replays", ctypes.c_uint32), ("graph_builds", ctypes.c_uint32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BlazeServerConfig(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32),
+                ("memory_budget", ctypes.c_uint64), ("batch_window_us", ctypes.c_uint32),
+                ("evalue", ctypes.c_double), ("tuning", BlazeTuning)]
+
+
+class BlazeServerStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+        ("residues", ctypes.c_uint64), ("latency_p50_ms", ctypes.c_double),
+        ("latency_p99_ms", ctypes.c_double), ("latency_max_ms", ctypes.c_double),
+        ("busy_s", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -123,6 +144,13 @@ def load(path: str | None = None):
     L.blaze_search_run_batch.argtypes = [vp, vp, ctypes.POINTER(BlazeParams), u64p]
     L.blaze_search_batch_results.argtypes = [vp, vp, ctypes.c_uint64, u64p]
     L.blaze_search_set_tuning.argtypes = [vp, ctypes.POINTER(BlazeTuning)]
+    L.blaze_server_create.argtypes = [vp, ctypes.POINTER(BlazeServerConfig), ctypes.POINTER(vp)]
+    L.blaze_server_submit.argtypes = [vp, u8p, i32, u64p]
+    L.blaze_server_wait.argtypes = [vp, ctypes.c_uint64, i32, u64p]
+    L.blaze_server_take.argtypes = [vp, ctypes.c_uint64, vp, ctypes.c_uint64, u64p,
+                                    ctypes.POINTER(ctypes.c_double)]
+    L.blaze_server_stats_get.argtypes = [vp, ctypes.POINTER(BlazeServerStats)]
+    L.blaze_server_free.argtypes = [vp]
     for name in EXPORTS:
         if name not in ("blaze_status_string", "blaze_last_cuda_error"):
             getattr(L, name).restype = ctypes.c_int

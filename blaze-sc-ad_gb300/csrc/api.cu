@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "internal.h"
 
 using namespace blaze;
 
@@ -21,6 +22,8 @@ constexpr uint32_t kInitialScratchCap = 1024;             // init hits per subje
 }  // namespace
 
 void last_cuda_error(cudaError_t e) { g_last_cuda = e; }
+int last_cuda_error_code() { return static_cast<int>(g_last_cuda); }
+void set_last_cuda_error_code(int code) { g_last_cuda = static_cast<cudaError_t>(code); }
 
 extern "C" const char *blaze_last_cuda_error(void) { return cudaGetErrorString(g_last_cuda); }
 
@@ -92,6 +95,11 @@ struct blaze_search {
     uint32_t stage_bytes = kScanStageBytes;
     uint32_t tile_subjects = kDefaultTileSubjects;
     uint32_t max_warps = 0;
+    uint32_t launch_mode = 0;
+    // the per-pass launch sequence as a CUDA graph, and the arguments it was
+    // captured with
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<unsigned char> graph_key;
     // batched runs
     unsigned long long work_cap = 0;
     DevBuf<BatchQuery> bq;
@@ -109,6 +117,10 @@ struct blaze_batch {
     int32_t threshold = 0;
     std::vector<int32_t> qlen;
     std::vector<uint64_t> res_off, off_off;  // per query: residues, hit lists
+    // device tables; a refilled batch keeps them while they are large enough
+    DevBuf<uint8_t> res;
+    DevBuf<uint32_t> cell_start, cell_pack, presence;
+    DevBuf<uint16_t> cell_off;
     uint8_t *d_res = nullptr;
     uint32_t *d_cell_start = nullptr, *d_cell_pack = nullptr, *d_presence = nullptr;
     uint16_t *d_cell_off = nullptr;
@@ -312,6 +324,7 @@ extern "C" int blaze_search_free(blaze_search *s) {
     if (!s) return BLAZE_OK;
     cudaSetDevice(s->db->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     s->scratch.release();
     s->init_out.release();
     s->sorted.release();
@@ -353,6 +366,89 @@ struct RunSpec {
 };
 
 // One pass of both stages; fills s->h_cnt.
+// One pass's launch sequence: counter reset, scan kernel, gapped kernel and
+// the counter read-back, with the timing events between them.
+struct PassLaunch {
+    const ScanArgs *sa;
+    const GappedArgs *ga;
+    bool batched;
+    int scan_blocks, warps_per_block;
+    size_t smem_bytes;
+};
+
+static cudaError_t enqueue_pass(blaze_search *s, const PassLaunch &pl, unsigned event_flags) {
+    cudaError_t e = cudaMemsetAsync(s->d_cnt, 0, sizeof(DevCounters), s->stream);
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(s->ev[1], s->stream, event_flags);
+    if (e == cudaSuccess)
+        e = pl.batched ? launch_scan_batch(*pl.sa, pl.scan_blocks, pl.warps_per_block, pl.smem_bytes, s->stream)
+                       : launch_scan(*pl.sa, pl.scan_blocks, pl.warps_per_block, pl.smem_bytes, s->stream);
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(s->ev[2], s->stream, event_flags);
+    if (e == cudaSuccess) e = launch_gapped(*pl.ga, s->gapped_blocks, s->stream);
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(s->ev[3], s->stream, event_flags);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->h_cnt, s->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, s->stream);
+    return e;
+}
+
+static int launch_pass_direct(blaze_search *s, const PassLaunch &pl) {
+    BLAZE_CUDA_TRY(enqueue_pass(s, pl, cudaEventRecordDefault));
+    return BLAZE_OK;
+}
+
+// Replays the pass from a CUDA graph. The graph's kernel arguments are the
+// ScanArgs/GappedArgs values themselves (every buffer they point to keeps its
+// address while it is not regrown), so a pass whose arguments and launch
+// shapes equal those of the captured one replays it; otherwise the sequence
+// is captured again and the executable graph updated in place (or rebuilt
+// when the update is refused). Capture is thread-local, so other host
+// threads may allocate meanwhile.
+static int launch_pass_graph(blaze_search *s, const PassLaunch &pl) {
+    std::vector<unsigned char> key(sizeof(ScanArgs) + sizeof(GappedArgs) + 4 * sizeof(int64_t));
+    unsigned char *k = key.data();
+    std::memcpy(k, pl.sa, sizeof(ScanArgs));
+    std::memcpy(k + sizeof(ScanArgs), pl.ga, sizeof(GappedArgs));
+    const int64_t shape[4] = {pl.batched, pl.scan_blocks * 4096ll + pl.warps_per_block,
+                              static_cast<int64_t>(pl.smem_bytes), s->gapped_blocks};
+    std::memcpy(k + sizeof(ScanArgs) + sizeof(GappedArgs), shape, sizeof(shape));
+    if (s->graph_exec && key == s->graph_key) {
+        BLAZE_CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
+        s->stats.graph_replays++;
+        return BLAZE_OK;
+    }
+    BLAZE_CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t e = enqueue_pass(s, pl, cudaEventRecordExternal);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s->stream, &g);
+    if (e != cudaSuccess || ec != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        s->graph_key.clear();
+        BLAZE_CUDA_TRY(e != cudaSuccess ? e : ec);
+    }
+    bool updated = false;
+    if (s->graph_exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(s->graph_exec, g, &info) == cudaSuccess) {
+            updated = true;
+        } else {
+            cudaGetLastError();  // a refused update is not an error: rebuild
+            cudaGraphExecDestroy(s->graph_exec);
+            s->graph_exec = nullptr;
+        }
+    }
+    cudaError_t ei = cudaSuccess;
+    if (!updated) ei = cudaGraphInstantiate(&s->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        s->graph_exec = nullptr;
+        s->graph_key.clear();
+        BLAZE_CUDA_TRY(ei);
+    }
+    s->graph_key.swap(key);
+    s->stats.graph_builds++;
+    BLAZE_CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
+    return BLAZE_OK;
+}
+
 static int run_pass(blaze_search *s, const RunSpec &r, const ScanLayout &lay, int scan_blocks) {
     const int warps_per_block = lay.warps_per_block;
     blaze_db *db = s->db;
@@ -375,9 +471,8 @@ static int run_pass(blaze_search *s, const RunSpec &r, const ScanLayout &lay, in
     const size_t dp_stride = static_cast<size_t>(std::max<uint32_t>(db->max_len, 1)) + 2;
     if ((rc = s->dp.ensure(gapped_warps * 2 * dp_stride)) != BLAZE_OK) return rc;
 
-    BLAZE_CUDA_TRY(cudaMemsetAsync(s->d_cnt, 0, sizeof(DevCounters), s->stream));
-    BLAZE_CUDA_TRY(cudaEventRecord(s->ev[1], s->stream));
-    ScanArgs sa{};
+    ScanArgs sa;
+    std::memset(&sa, 0, sizeof(sa));  // whole bytes: the graph key compares them
     sa.res = db->d_res;
     sa.off = db->d_off;
     sa.n_subj = db->n;
@@ -402,7 +497,6 @@ static int run_pass(blaze_search *s, const RunSpec &r, const ScanLayout &lay, in
         sa.n_queries = r.b->n;
         sa.tile_subjects = s->tile_subjects;
         sa.work_query = s->work_query.p;
-        BLAZE_CUDA_TRY(launch_scan_batch(sa, scan_blocks, warps_per_block, lay.smem_bytes, s->stream));
     } else {
         const blaze_query *q = r.q;
         sa.q = q->d_q;
@@ -413,11 +507,10 @@ static int run_pass(blaze_search *s, const RunSpec &r, const ScanLayout &lay, in
         sa.cell_off = q->d_cell_off;
         sa.cutoff = p->ungapped_cutoff;
         sa.n_queries = 1;
-        BLAZE_CUDA_TRY(launch_scan(sa, scan_blocks, warps_per_block, lay.smem_bytes, s->stream));
     }
-    BLAZE_CUDA_TRY(cudaEventRecord(s->ev[2], s->stream));
 
-    GappedArgs ga{};
+    GappedArgs ga;
+    std::memset(&ga, 0, sizeof(ga));
     ga.res = db->d_res;
     ga.off = db->d_off;
     ga.init_in = s->init_out.p;
@@ -445,11 +538,11 @@ static int run_pass(blaze_search *s, const RunSpec &r, const ScanLayout &lay, in
         ga.qlen = r.q->qlen;
         ga.cutoff = p->gapped_cutoff;
     }
-    BLAZE_CUDA_TRY(launch_gapped(ga, s->gapped_blocks, s->stream));
-    BLAZE_CUDA_TRY(cudaEventRecord(s->ev[3], s->stream));
+    PassLaunch pl{&sa, &ga, batched, scan_blocks, warps_per_block, lay.smem_bytes};
+    const bool graph = s->launch_mode == 2 || (s->launch_mode == 0 && batched);
+    if ((rc = graph ? launch_pass_graph(s, pl) : launch_pass_direct(s, pl)) != BLAZE_OK) return rc;
     s->stats.kernel_launches += 2;
     s->stats.d2h_bytes += sizeof(DevCounters);
-    BLAZE_CUDA_TRY(cudaMemcpyAsync(s->h_cnt, s->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, s->stream));
     BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
     return BLAZE_OK;
 }
@@ -706,6 +799,8 @@ extern "C" int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t) {
     if (!s || !t) return BLAZE_ERR_INVALID_ARG;
     if (t->stage_bytes > 16384 || t->max_warps_per_block > static_cast<uint32_t>(kScanMaxWarpsPerBlock))
         return BLAZE_ERR_LIMIT;
+    if (t->launch_mode > 2) return BLAZE_ERR_INVALID_ARG;
+    s->launch_mode = t->launch_mode;
     s->stage_bytes = t->stage_bytes ? t->stage_bytes : kScanStageBytes;
     s->tile_subjects = t->tile_subjects ? t->tile_subjects : kDefaultTileSubjects;
     s->max_warps = t->max_warps_per_block;
@@ -730,20 +825,27 @@ extern "C" int blaze_search_stats(const blaze_search *s, blaze_stats *out) {
     return BLAZE_OK;
 }
 
-extern "C" int blaze_batch_create(const blaze_db *db, const uint8_t *residues, const uint64_t *offsets,
-                                  uint32_t n_queries, int32_t word_threshold, blaze_batch **out) {
-    if (!db || !residues || !offsets || !out || n_queries == 0) return BLAZE_ERR_INVALID_ARG;
-    *out = nullptr;
+static int check_batch_input(const uint8_t *residues, const uint64_t *offsets, uint32_t n_queries) {
+    if (!residues || !offsets || n_queries == 0) return BLAZE_ERR_INVALID_ARG;
     for (uint32_t i = 0; i < n_queries; ++i) {
         if (offsets[i + 1] <= offsets[i]) return BLAZE_ERR_INVALID_ARG;
         if (offsets[i + 1] - offsets[i] > static_cast<uint64_t>(kMaxQueryLength)) return BLAZE_ERR_LIMIT;
         if (!valid_residues(residues + offsets[i], offsets[i + 1] - offsets[i])) return BLAZE_ERR_INVALID_ARG;
     }
-    BLAZE_CUDA_TRY(cudaSetDevice(db->device));
-    auto *b = new blaze_batch();
-    b->device = db->device;
+    return BLAZE_OK;
+}
+
+// Builds the word tables of every query on the host and uploads them into
+// the batch's device buffers, growing those only when they are too small
+// (so that a refilled batch allocates nothing once it has seen its largest
+// load). Copies go on `stream` (0: synchronous).
+static int batch_fill(blaze_batch *b, const uint8_t *residues, const uint64_t *offsets, uint32_t n_queries,
+                      int32_t word_threshold, cudaStream_t stream) {
     b->n = n_queries;
     b->threshold = word_threshold;
+    b->qlen.clear();
+    b->res_off.clear();
+    b->off_off.clear();
     std::vector<uint8_t> res;
     std::vector<uint32_t> cs_all(static_cast<size_t>(n_queries) * (kWords + 1));
     std::vector<uint32_t> pack_all(static_cast<size_t>(n_queries) * kWords);
@@ -760,10 +862,7 @@ extern "C" int blaze_batch_create(const blaze_db *db, const uint8_t *residues, c
         uint16_t *offs = nullptr;
         uint32_t n_off = 0;
         int rc = build_lookup(q, len, word_threshold, cs, &offs, &n_off);
-        if (rc != BLAZE_OK) {
-            delete b;
-            return rc;
-        }
+        if (rc != BLAZE_OK) return rc;
         b->off_off.push_back(offs_all.size());
         offs_all.insert(offs_all.end(), offs, offs + n_off);
         std::free(offs);
@@ -777,36 +876,83 @@ extern "C" int blaze_batch_create(const blaze_db *db, const uint8_t *residues, c
     }
     res.resize(res.size() + 64, 0);
     if (offs_all.empty()) offs_all.push_back(0);
-    cudaError_t e = cudaMalloc(&b->d_res, res.size());
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_cell_start, sizeof(uint32_t) * cs_all.size());
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_cell_pack, sizeof(uint32_t) * pack_all.size());
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_presence, sizeof(uint32_t) * pres_all.size());
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_cell_off, sizeof(uint16_t) * offs_all.size());
-    if (e == cudaSuccess) e = cudaMemcpy(b->d_res, res.data(), res.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(b->d_cell_start, cs_all.data(), sizeof(uint32_t) * cs_all.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(b->d_cell_pack, pack_all.data(), sizeof(uint32_t) * pack_all.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(b->d_presence, pres_all.data(), sizeof(uint32_t) * pres_all.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(b->d_cell_off, offs_all.data(), sizeof(uint16_t) * offs_all.size(), cudaMemcpyHostToDevice);
+    // a refill grows by half again so that slowly rising loads settle
+    const size_t slack = stream ? 2 : 1;
+    auto grow = [&](auto &buf, size_t want) {
+        return want <= buf.n ? BLAZE_OK : buf.ensure(want + (slack - 1) * want / 2);
+    };
+    int rc = grow(b->res, res.size());
+    if (rc == BLAZE_OK) rc = grow(b->cell_start, cs_all.size());
+    if (rc == BLAZE_OK) rc = grow(b->cell_pack, pack_all.size());
+    if (rc == BLAZE_OK) rc = grow(b->presence, pres_all.size());
+    if (rc == BLAZE_OK) rc = grow(b->cell_off, offs_all.size());
+    if (rc != BLAZE_OK) return rc;
+    b->d_res = b->res.p;
+    b->d_cell_start = b->cell_start.p;
+    b->d_cell_pack = b->cell_pack.p;
+    b->d_presence = b->presence.p;
+    b->d_cell_off = b->cell_off.p;
+    auto put = [&](void *dst, const void *src, size_t bytes) {
+        return stream ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream)
+                      : cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    cudaError_t e = put(b->d_res, res.data(), res.size());
+    if (e == cudaSuccess) e = put(b->d_cell_start, cs_all.data(), sizeof(uint32_t) * cs_all.size());
+    if (e == cudaSuccess) e = put(b->d_cell_pack, pack_all.data(), sizeof(uint32_t) * pack_all.size());
+    if (e == cudaSuccess) e = put(b->d_presence, pres_all.data(), sizeof(uint32_t) * pres_all.size());
+    if (e == cudaSuccess) e = put(b->d_cell_off, offs_all.data(), sizeof(uint16_t) * offs_all.size());
+    // the host arrays die with this frame: the copies must have read them
+    if (e == cudaSuccess && stream) e = cudaStreamSynchronize(stream);
     b->upload_bytes = res.size() + sizeof(uint32_t) * (cs_all.size() + pack_all.size() + pres_all.size()) +
                       sizeof(uint16_t) * offs_all.size();
-    b->device_bytes = b->upload_bytes;
+    b->device_bytes = b->res.n + sizeof(uint32_t) * (b->cell_start.n + b->cell_pack.n + b->presence.n) +
+                      sizeof(uint16_t) * b->cell_off.n;
     if (e != cudaSuccess) {
         last_cuda_error(e);
-        blaze_batch_free(b);
         return e == cudaErrorMemoryAllocation ? BLAZE_ERR_OUT_OF_MEMORY : BLAZE_ERR_CUDA;
+    }
+    return BLAZE_OK;
+}
+
+extern "C" int blaze_batch_create(const blaze_db *db, const uint8_t *residues, const uint64_t *offsets,
+                                  uint32_t n_queries, int32_t word_threshold, blaze_batch **out) {
+    if (!db || !out) return BLAZE_ERR_INVALID_ARG;
+    *out = nullptr;
+    const int vrc = check_batch_input(residues, offsets, n_queries);
+    if (vrc != BLAZE_OK) return vrc;
+    BLAZE_CUDA_TRY(cudaSetDevice(db->device));
+    auto *b = new blaze_batch();
+    b->device = db->device;
+    const int rc = batch_fill(b, residues, offsets, n_queries, word_threshold, nullptr);
+    if (rc != BLAZE_OK) {
+        blaze_batch_free(b);
+        return rc;
     }
     *out = b;
     return BLAZE_OK;
 }
 
+int batch_refill(blaze_search *s, blaze_batch **inout, const uint8_t *residues, const uint64_t *offsets,
+                 uint32_t n_queries, int32_t word_threshold) {
+    if (!s || !inout) return BLAZE_ERR_INVALID_ARG;
+    const int vrc = check_batch_input(residues, offsets, n_queries);
+    if (vrc != BLAZE_OK) return vrc;
+    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
+    if (!*inout) {
+        *inout = new blaze_batch();
+        (*inout)->device = s->db->device;
+    }
+    return batch_fill(*inout, residues, offsets, n_queries, word_threshold, s->stream);
+}
+
 extern "C" int blaze_batch_free(blaze_batch *b) {
     if (!b) return BLAZE_OK;
     cudaSetDevice(b->device);
-    if (b->d_res) cudaFree(b->d_res);
-    if (b->d_cell_start) cudaFree(b->d_cell_start);
-    if (b->d_cell_pack) cudaFree(b->d_cell_pack);
-    if (b->d_presence) cudaFree(b->d_presence);
-    if (b->d_cell_off) cudaFree(b->d_cell_off);
+    b->res.release();
+    b->cell_start.release();
+    b->cell_pack.release();
+    b->presence.release();
+    b->cell_off.release();
     delete b;
     return BLAZE_OK;
 }

@@ -1,0 +1,17 @@
+// internal.h -- calls between the library's own translation units that are
+// not part of the C ABI.
+#pragma once
+#include <cstdint>
+
+#include "blaze_prelim.h"
+
+// Refills (creating it when *batch is null) a batch with new queries on the
+// search context's stream, reusing its device buffers while they are large
+// enough; validation and results as blaze_batch_create.
+int batch_refill(blaze_search *s, blaze_batch **batch, const uint8_t *residues, const uint64_t *offsets,
+                 uint32_t n_queries, int32_t word_threshold);
+
+// The calling thread's last CUDA error (as a cudaError_t value), so that a
+// worker thread's error can be handed to the thread that reads the status.
+int last_cuda_error_code();
+void set_last_cuda_error_code(int code);

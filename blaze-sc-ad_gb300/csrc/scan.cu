@@ -14,6 +14,9 @@
 // sequential algorithm.
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
+#include <set>
+#include <utility>
 
 #include "common.cuh"
 
@@ -569,10 +572,28 @@ ScanLayout scan_layout(int32_t qlen, int32_t window, uint32_t stage_bytes, size_
     return l;
 }
 
+// Opts a scan kernel in to the device's full dynamic shared memory, once per
+// (device, kernel). The attribute is process-wide: setting it per launch to
+// that launch's size would let one host thread lower it between another
+// thread's setting and launch, and that launch would then fail.
+static cudaError_t allow_full_smem(const void *kernel) {
+    static std::mutex mu;
+    static std::set<std::pair<int, const void *>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count({dev, kernel})) return cudaSuccess;
+    int optin = 0;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess) done.insert({dev, kernel});
+    return e;
+}
+
 cudaError_t launch_scan(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem_bytes, cudaStream_t st) {
     auto kernel = a.query_smem_bytes ? scan_kernel<true> : scan_kernel<false>;
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem_bytes));
+    cudaError_t e = allow_full_smem(reinterpret_cast<const void *>(kernel));
     if (e != cudaSuccess) return e;
     kernel<<<n_blocks, warps_per_block * 32, smem_bytes, st>>>(a);
     return cudaGetLastError();
@@ -592,16 +613,14 @@ int scan_max_warps_by_registers(bool query_in_smem) {
 
 cudaError_t launch_scan_batch(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem_bytes,
                               cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(scan_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem_bytes));
+    cudaError_t e = allow_full_smem(reinterpret_cast<const void *>(scan_batch_kernel));
     if (e != cudaSuccess) return e;
     scan_batch_kernel<<<n_blocks, warps_per_block * 32, smem_bytes, st>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t scan_batch_occupancy(int warps_per_block, size_t smem_bytes, int *blocks_per_sm) {
-    cudaError_t e = cudaFuncSetAttribute(scan_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem_bytes));
+    cudaError_t e = allow_full_smem(reinterpret_cast<const void *>(scan_batch_kernel));
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, scan_batch_kernel, warps_per_block * 32,
                                                          smem_bytes);
@@ -619,8 +638,7 @@ int scan_batch_max_warps_by_registers() {
 
 cudaError_t scan_occupancy(bool query_in_smem, int warps_per_block, size_t smem_bytes, int *blocks_per_sm) {
     auto kernel = query_in_smem ? scan_kernel<true> : scan_kernel<false>;
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem_bytes));
+    cudaError_t e = allow_full_smem(reinterpret_cast<const void *>(kernel));
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel, warps_per_block * 32,
                                                          smem_bytes);

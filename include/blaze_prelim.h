@@ -105,6 +105,8 @@ typedef struct blaze_stats {
     uint32_t kernel_launches; /* kernels launched by the run, all passes */
     uint64_t h2d_bytes; /* host->device bytes of the run (query tables included) */
     uint64_t d2h_bytes; /* device->host bytes of the run */
+    uint32_t graph_replays; /* passes launched from an already built CUDA graph */
+    uint32_t graph_builds;  /* passes that captured (or updated) the CUDA graph */
 } blaze_stats;
 
 const char *blaze_status_string(int status);
@@ -199,8 +201,55 @@ typedef struct blaze_tuning {
     uint32_t stage_bytes;
     uint32_t tile_subjects;
     uint32_t max_warps_per_block;
+    /* 0: the per-pass launch sequence (counter reset, scan, gapped, counter
+     * read-back) runs as a CUDA graph for batched runs and as direct launches
+     * for single queries; 1: direct launches always; 2: CUDA graph always.
+     * The graph is captured once and replayed while the launch arguments stay
+     * the same (updated in place when they change). */
+    uint32_t launch_mode;
 } blaze_tuning;
 int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t);
+
+/* ---------------------------------------------------------------------
+ * Serving loop: continuous batching over the resident database. Queries are
+ * submitted as they arrive; `slots` worker threads (each with its own search
+ * context and CUDA stream) take the waiting queries into their next batch
+ * as soon as they are free, admitting queries while the device memory of
+ * the in-flight batches (word tables plus a per-query allowance for seed and
+ * HSP buffers) stays within memory_budget, so batches overlap on the GPU.
+ * Each query's HSP lists are handed back when its batch completes.
+ */
+typedef struct blaze_server blaze_server;
+
+typedef struct blaze_server_config {
+    uint32_t slots;           /* batches in flight at once (>= 1) */
+    uint32_t max_batch;       /* queries per batch at most (>= 1) */
+    uint64_t memory_budget;   /* bytes for in-flight batches (0: no limit) */
+    uint32_t batch_window_us; /* after the first waiting query, wait this long for more */
+    double evalue;            /* expect value for every query's default parameters */
+    blaze_tuning tuning;      /* launch shape of every worker's search (zeros: defaults) */
+} blaze_server_config;
+
+typedef struct blaze_server_stats {
+    uint64_t submitted, completed, batches;
+    uint64_t residues;        /* query x database residues completed */
+    double latency_p50_ms, latency_p99_ms, latency_max_ms;
+    double busy_s;            /* wall time from first submit to last completion */
+} blaze_server_stats;
+
+int blaze_server_create(blaze_db *db, const blaze_server_config *cfg, blaze_server **out);
+/* Queues one query; *ticket identifies it. Thread-safe. */
+int blaze_server_submit(blaze_server *srv, const uint8_t *query, int32_t length, uint64_t *ticket);
+/* Blocks until the ticket's batch completed (timeout_ms < 0: no limit);
+ * returns BLAZE_ERR_LIMIT on timeout. *n_hsps is its HSP count. */
+int blaze_server_wait(blaze_server *srv, uint64_t ticket, int32_t timeout_ms, uint64_t *n_hsps);
+/* Copies a completed ticket's HSPs (grouped by OID, NCBI order), its latency
+ * from submission to completion, and releases the ticket. */
+int blaze_server_take(blaze_server *srv, uint64_t ticket, blaze_hsp *out, uint64_t capacity,
+                      uint64_t *n_hsps, double *latency_ms);
+int blaze_server_stats_get(blaze_server *srv, blaze_server_stats *out);
+/* Finishes every queued query, stops the workers and frees the server. */
+int blaze_server_free(blaze_server *srv);
 
 /* Convenience: blaze_query_create + blaze_search_run + blaze_search_results
  * in one call with host buffers (the drop-in path). */

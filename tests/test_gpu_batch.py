@@ -105,3 +105,41 @@ def test_batch_rejects_mixed_search_settings():
     batch.close()
     ps.close()
     db.close()
+
+
+def test_graph_replay_matches_direct_launches():
+    qs = _queries(lengths=(40, 300, 700, 1200))
+    res, off = _db(n=1500, with_homologs_of=qs)
+    db = blaze103.SeqSrc(res, off)
+    ps = blaze103.PrelimSearch(db)
+    params = [params_for(len(q), db.tot_len, db.num_seqs)[0] for q in qs]
+    ps.set_tuning(launch_mode=1)
+    batch = blaze103.QueryBatch(db, qs)
+    direct = ps.run_batch(batch, params)
+    assert ps.stats()["graph_builds"] == 0 and ps.stats()["graph_replays"] == 0
+    ps.set_tuning(launch_mode=0)  # batched runs go through the graph
+    first = ps.run_batch(batch, params)
+    assert ps.stats()["graph_builds"] == 1
+    again = ps.run_batch(batch, params)
+    assert ps.stats()["graph_replays"] == 1 and ps.stats()["graph_builds"] == 0
+    assert np.array_equal(first, direct) and np.array_equal(again, direct)
+    # a different batch changes the arguments: the graph is updated, not reused
+    sub = blaze103.QueryBatch(db, qs[1:3])
+    got = ps.run_batch(sub, params[1:3])
+    assert ps.stats()["graph_builds"] >= 1
+    for i in range(2):
+        w = direct[direct["query"] == i + 1]
+        g = got[got["query"] == i]
+        for f in blaze103.HSP_DTYPE.names:
+            assert np.array_equal(g[f], w[f]), f
+    # single queries through the graph as well
+    ps.set_tuning(launch_mode=2)
+    one = ps.run(qs[2], params[2]).hsps
+    ps.set_tuning(launch_mode=1)
+    assert np.array_equal(one, ps.run(qs[2], params[2]).hsps)
+    with pytest.raises(blaze103.BlazeError):
+        ps.set_tuning(launch_mode=3)
+    sub.close()
+    batch.close()
+    ps.close()
+    db.close()
