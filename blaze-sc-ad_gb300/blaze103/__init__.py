@@ -232,15 +232,15 @@ class PrelimSearch:
         finally:
             q.close()
 
-    def set_tuning(self, stage_bytes: int = 0, tile_subjects: int = 0, max_warps_per_block: int = 0,
+    def set_tuning(self, stage_bytes: int = 0, tile_residues: int = 0, max_warps_per_block: int = 0,
                    launch_mode: int = 0):
         """Launch shape (0 = library default for each); launch_mode 0: CUDA
         graph for batched runs, 1: direct launches, 2: CUDA graph always."""
         self._auto = False
-        self._set_tuning(stage_bytes, tile_subjects, max_warps_per_block, launch_mode)
+        self._set_tuning(stage_bytes, tile_residues, max_warps_per_block, launch_mode)
 
-    def _set_tuning(self, stage_bytes=0, tile_subjects=0, max_warps_per_block=0, launch_mode=0):
-        t = BlazeTuning(int(stage_bytes), int(tile_subjects), int(max_warps_per_block), int(launch_mode))
+    def _set_tuning(self, stage_bytes=0, tile_residues=0, max_warps_per_block=0, launch_mode=0):
+        t = BlazeTuning(int(stage_bytes), int(tile_residues), int(max_warps_per_block), int(launch_mode))
         check(self._lib.blaze_search_set_tuning(self._h, ctypes.byref(t)), "blaze_search_set_tuning")
 
     @property

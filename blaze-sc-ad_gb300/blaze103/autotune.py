@@ -4,7 +4,7 @@ For each named shape (a query-length profile, a batch size and a database
 size) it times the search over a grid of launch settings with CUDA events --
 the subject staging bound (subjects up to `stage_bytes` residues are staged in
 shared memory, longer ones are read from global memory), warps per scan block
-and subjects per batched tile -- checks that every setting returns the same
+and residues per batched tile -- checks that every setting returns the same
 HSPs, and writes the fastest setting per shape to ``tuning.json`` beside this
 file. ``lookup`` returns the entry of the nearest shape; ``PrelimSearch``
 applies it to batched runs unless a tuning was set explicitly.
@@ -37,7 +37,7 @@ SHAPES = {
 GRID = {
     "stage_bytes": (1024, 2048, 4096),
     "max_warps_per_block": (8, 16, 0),  # 0: as many as registers allow
-    "tile_subjects": (64, 256, 1024),
+    "tile_residues": (0, 4096, 65536),  # 0: several tiles per warp
 }
 
 _cache = None
@@ -113,7 +113,7 @@ def tune_shape(name: str, reps: int = 3, quick: bool = False) -> dict:
 
     grid = dict(GRID)
     if kind == "plain":
-        grid["tile_subjects"] = (256,)  # single-query runs have no tiles
+        grid["tile_residues"] = (0,)  # single-query runs have no tiles
     if quick:
         grid = {k: v[:2] for k, v in grid.items()}
     rows, ref = [], None
@@ -140,7 +140,7 @@ def tune_shape(name: str, reps: int = 3, quick: bool = False) -> dict:
              "tuning": rows[0]["tuning"], "ms": rows[0]["ms"],
              "default_ms": next((r["ms"] for r in rows if r["tuning"] == {
                  "stage_bytes": 2048, "max_warps_per_block": 0,
-                 "tile_subjects": 256}), None),
+                 "tile_residues": 0}), None),
              "grid": rows}
     if kind == "batched":
         batch.close()

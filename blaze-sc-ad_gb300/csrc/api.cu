@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <numeric>
 #include <vector>
 
@@ -35,6 +36,7 @@ struct blaze_db {
     uint32_t n = 0;
     uint32_t max_len = 0;
     std::vector<uint32_t> oid_of;  // sorted index -> OID
+    std::vector<uint64_t> h_off;   // offsets of the length-sorted copy (host)
 };
 
 struct blaze_query {
@@ -93,7 +95,10 @@ struct blaze_search {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // launch shape (blaze_search_set_tuning)
     uint32_t stage_bytes = kScanStageBytes;
-    uint32_t tile_subjects = kDefaultTileSubjects;
+    uint32_t tile_residues = 0;  // 0: automatic
+    // residue-balanced subject ranges of batched tiles, per tile size
+    std::map<uint32_t, DevBuf<uint32_t>> tile_bounds;
+    std::map<uint32_t, uint32_t> tile_ranges;
     uint32_t max_warps = 0;
     uint32_t launch_mode = 0;
     // the per-pass launch sequence as a CUDA graph, and the arguments it was
@@ -106,6 +111,7 @@ struct blaze_search {
     DevBuf<const uint8_t *> bqptr;
     DevBuf<int32_t> bqlen, bcut;
     DevBuf<uint32_t> work_query, out_query;
+    DevBuf<unsigned long long> cursors;  // one work cursor per scan launch of a pass
     uint32_t *h_outq = nullptr;  // pinned
     size_t h_outq_n = 0;
     std::vector<blaze_batch_hsp> batch_results;
@@ -207,6 +213,7 @@ extern "C" int blaze_db_create(int device, const uint8_t *residues, const uint64
         blaze_db_free(db);
         return rc;
     }
+    db->h_off.swap(off);
     *out = db;
     return BLAZE_OK;
 }
@@ -325,6 +332,7 @@ extern "C" int blaze_search_free(blaze_search *s) {
     cudaSetDevice(s->db->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    for (auto &kv : s->tile_bounds) kv.second.release();
     s->scratch.release();
     s->init_out.release();
     s->sorted.release();
@@ -338,6 +346,7 @@ extern "C" int blaze_search_free(blaze_search *s) {
     s->bcut.release();
     s->work_query.release();
     s->out_query.release();
+    s->cursors.release();
     if (s->h_outq) cudaFreeHost(s->h_outq);
     if (s->d_cnt) cudaFree(s->d_cnt);
     if (s->h_cnt) cudaFreeHost(s->h_cnt);
@@ -368,20 +377,28 @@ struct RunSpec {
 // One pass of both stages; fills s->h_cnt.
 // One pass's launch sequence: counter reset, scan kernel, gapped kernel and
 // the counter read-back, with the timing events between them.
+struct ScanLaunch {
+    ScanArgs sa;
+    int blocks, warps_per_block;
+    size_t smem_bytes;
+};
+
 struct PassLaunch {
-    const ScanArgs *sa;
+    std::vector<ScanLaunch> scans;
     const GappedArgs *ga;
     bool batched;
-    int scan_blocks, warps_per_block;
-    size_t smem_bytes;
 };
 
 static cudaError_t enqueue_pass(blaze_search *s, const PassLaunch &pl, unsigned event_flags) {
     cudaError_t e = cudaMemsetAsync(s->d_cnt, 0, sizeof(DevCounters), s->stream);
-    if (e == cudaSuccess) e = cudaEventRecordWithFlags(s->ev[1], s->stream, event_flags);
     if (e == cudaSuccess)
-        e = pl.batched ? launch_scan_batch(*pl.sa, pl.scan_blocks, pl.warps_per_block, pl.smem_bytes, s->stream)
-                       : launch_scan(*pl.sa, pl.scan_blocks, pl.warps_per_block, pl.smem_bytes, s->stream);
+        e = cudaMemsetAsync(s->cursors.p, 0, sizeof(unsigned long long) * pl.scans.size(), s->stream);
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(s->ev[1], s->stream, event_flags);
+    for (const ScanLaunch &l : pl.scans) {
+        if (e != cudaSuccess) break;
+        e = pl.batched ? launch_scan_batch(l.sa, l.blocks, l.warps_per_block, l.smem_bytes, s->stream)
+                       : launch_scan(l.sa, l.blocks, l.warps_per_block, l.smem_bytes, s->stream);
+    }
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(s->ev[2], s->stream, event_flags);
     if (e == cudaSuccess) e = launch_gapped(*pl.ga, s->gapped_blocks, s->stream);
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(s->ev[3], s->stream, event_flags);
@@ -403,13 +420,19 @@ static int launch_pass_direct(blaze_search *s, const PassLaunch &pl) {
 // when the update is refused). Capture is thread-local, so other host
 // threads may allocate meanwhile.
 static int launch_pass_graph(blaze_search *s, const PassLaunch &pl) {
-    std::vector<unsigned char> key(sizeof(ScanArgs) + sizeof(GappedArgs) + 4 * sizeof(int64_t));
-    unsigned char *k = key.data();
-    std::memcpy(k, pl.sa, sizeof(ScanArgs));
-    std::memcpy(k + sizeof(ScanArgs), pl.ga, sizeof(GappedArgs));
-    const int64_t shape[4] = {pl.batched, pl.scan_blocks * 4096ll + pl.warps_per_block,
-                              static_cast<int64_t>(pl.smem_bytes), s->gapped_blocks};
-    std::memcpy(k + sizeof(ScanArgs) + sizeof(GappedArgs), shape, sizeof(shape));
+    std::vector<unsigned char> key;
+    auto put = [&key](const void *p, size_t n) {
+        const auto *c = static_cast<const unsigned char *>(p);
+        key.insert(key.end(), c, c + n);
+    };
+    const int64_t head[2] = {pl.batched, s->gapped_blocks};
+    put(head, sizeof(head));
+    for (const ScanLaunch &l : pl.scans) {
+        put(&l.sa, sizeof(ScanArgs));
+        const int64_t shape[3] = {l.blocks, l.warps_per_block, static_cast<int64_t>(l.smem_bytes)};
+        put(shape, sizeof(shape));
+    }
+    put(pl.ga, sizeof(GappedArgs));
     if (s->graph_exec && key == s->graph_key) {
         BLAZE_CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
         s->stats.graph_replays++;
@@ -449,12 +472,56 @@ static int launch_pass_graph(blaze_search *s, const PassLaunch &pl) {
     return BLAZE_OK;
 }
 
-static int run_pass(blaze_search *s, const RunSpec &r, const ScanLayout &lay, int scan_blocks) {
-    const int warps_per_block = lay.warps_per_block;
+// One scan launch of a pass: the single-query kernel, or the batched kernel
+// over one length class of a batch (queries [first, first + n) of the
+// class-ordered descriptors), each with its own shared-memory layout.
+struct ScanPlan {
+    ScanLayout lay;
+    int blocks = 0;
+    uint32_t first = 0, n = 1;
+    uint32_t tile_residues = 0;
+};
+
+// Subject ranges of about `target` residues, from the longest subjects down
+// (bounds descending, n_ranges + 1 of them), uploaded once per tile size.
+static int tile_bounds_for(blaze_search *s, uint32_t target, const uint32_t **bounds, uint32_t *n_ranges) {
+    auto it = s->tile_bounds.find(target);
+    if (it == s->tile_bounds.end()) {
+        const std::vector<uint64_t> &off = s->db->h_off;
+        const uint32_t n = s->db->n;
+        std::vector<uint32_t> b{n};
+        for (uint32_t hi = n; hi > 0;) {
+            const uint64_t want = off[hi] > target ? off[hi] - target : 0;
+            uint32_t lo = static_cast<uint32_t>(std::lower_bound(off.begin(), off.begin() + hi, want) - off.begin());
+            if (lo >= hi) lo = hi - 1;
+            b.push_back(lo);
+            hi = lo;
+        }
+        DevBuf<uint32_t> d;
+        int rc = d.ensure(b.size());
+        if (rc != BLAZE_OK) return rc;
+        cudaError_t e = cudaMemcpy(d.p, b.data(), sizeof(uint32_t) * b.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            d.release();
+            BLAZE_CUDA_TRY(e);
+        }
+        s->stats.h2d_bytes += sizeof(uint32_t) * b.size();
+        it = s->tile_bounds.emplace(target, d).first;
+        s->tile_ranges[target] = static_cast<uint32_t>(b.size() - 1);
+    }
+    *bounds = it->second.p;
+    *n_ranges = s->tile_ranges[target];
+    return BLAZE_OK;
+}
+
+// One pass of both stages; fills s->h_cnt.
+static int run_pass(blaze_search *s, const RunSpec &r, const std::vector<ScanPlan> &plans) {
     blaze_db *db = s->db;
     const blaze_params *p = r.p;
     const bool batched = r.b != nullptr;
-    const size_t scan_warps = static_cast<size_t>(scan_blocks) * warps_per_block;
+    size_t scan_warps = 0;
+    for (const ScanPlan &pl : plans)
+        scan_warps = std::max(scan_warps, static_cast<size_t>(pl.blocks) * pl.lay.warps_per_block);
     const size_t gapped_warps = static_cast<size_t>(s->gapped_blocks) * kGappedWarpsPerBlock;
     const size_t work_cap = batched ? s->work_cap : std::max<uint32_t>(db->n, 1);
     int rc;
@@ -470,43 +537,55 @@ static int run_pass(blaze_search *s, const RunSpec &r, const ScanLayout &lay, in
     }
     const size_t dp_stride = static_cast<size_t>(std::max<uint32_t>(db->max_len, 1)) + 2;
     if ((rc = s->dp.ensure(gapped_warps * 2 * dp_stride)) != BLAZE_OK) return rc;
+    if ((rc = s->cursors.ensure(plans.size())) != BLAZE_OK) return rc;
 
-    ScanArgs sa;
-    std::memset(&sa, 0, sizeof(sa));  // whole bytes: the graph key compares them
-    sa.res = db->d_res;
-    sa.off = db->d_off;
-    sa.n_subj = db->n;
-    sa.window = p->window;
-    sa.xdrop = p->ungapped_xdrop;
-    sa.diag_entries = lay.diag_entries;
-    sa.diag_magic = lay.diag_magic;
-    sa.diag_bytes = lay.diag_bytes;
-    sa.diag_entries_max = lay.diag_entries;
-    sa.stage_bytes = lay.stage_bytes;
-    sa.query_smem_bytes = lay.query_smem_bytes;
-    sa.warp_smem_bytes = lay.warp_smem_bytes;
-    sa.scratch = s->scratch.p;
-    sa.scratch_cap = s->scratch_cap;
-    sa.init_out = s->init_out.p;
-    sa.init_cap = s->init_cap;
-    sa.work = s->work.p;
-    sa.work_cap = work_cap;
-    sa.cnt = s->d_cnt;
-    if (batched) {
-        sa.queries = s->bq.p;
-        sa.n_queries = r.b->n;
-        sa.tile_subjects = s->tile_subjects;
-        sa.work_query = s->work_query.p;
-    } else {
-        const blaze_query *q = r.q;
-        sa.q = q->d_q;
-        sa.qlen = q->qlen;
-        sa.cell_start = q->d_cell_start;
-        sa.cell_pack = q->d_cell_pack;
-        sa.presence = q->d_presence;
-        sa.cell_off = q->d_cell_off;
-        sa.cutoff = p->ungapped_cutoff;
-        sa.n_queries = 1;
+    PassLaunch pl;
+    pl.batched = batched;
+    for (const ScanPlan &plan : plans) {
+        const ScanLayout &lay = plan.lay;
+        ScanLaunch l;
+        ScanArgs &sa = l.sa;
+        std::memset(&sa, 0, sizeof(sa));  // whole bytes: the graph key compares them
+        l.blocks = plan.blocks;
+        l.warps_per_block = lay.warps_per_block;
+        l.smem_bytes = lay.smem_bytes;
+        sa.res = db->d_res;
+        sa.off = db->d_off;
+        sa.n_subj = db->n;
+        sa.window = p->window;
+        sa.xdrop = p->ungapped_xdrop;
+        sa.diag_entries = lay.diag_entries;
+        sa.diag_magic = lay.diag_magic;
+        sa.diag_bytes = lay.diag_bytes;
+        sa.diag_entries_max = lay.diag_entries;
+        sa.stage_bytes = lay.stage_bytes;
+        sa.query_smem_bytes = lay.query_smem_bytes;
+        sa.warp_smem_bytes = lay.warp_smem_bytes;
+        sa.scratch = s->scratch.p;
+        sa.scratch_cap = s->scratch_cap;
+        sa.init_out = s->init_out.p;
+        sa.init_cap = s->init_cap;
+        sa.work = s->work.p;
+        sa.work_cap = work_cap;
+        sa.cnt = s->d_cnt;
+        sa.cursor = s->cursors.p + pl.scans.size();
+        if (batched) {
+            sa.queries = s->bq.p + plan.first;
+            sa.n_queries = plan.n;
+            if ((rc = tile_bounds_for(s, plan.tile_residues, &sa.tile_bounds, &sa.n_ranges)) != BLAZE_OK) return rc;
+            sa.work_query = s->work_query.p;
+        } else {
+            const blaze_query *q = r.q;
+            sa.q = q->d_q;
+            sa.qlen = q->qlen;
+            sa.cell_start = q->d_cell_start;
+            sa.cell_pack = q->d_cell_pack;
+            sa.presence = q->d_presence;
+            sa.cell_off = q->d_cell_off;
+            sa.cutoff = p->ungapped_cutoff;
+            sa.n_queries = 1;
+        }
+        pl.scans.push_back(l);
     }
 
     GappedArgs ga;
@@ -538,10 +617,10 @@ static int run_pass(blaze_search *s, const RunSpec &r, const ScanLayout &lay, in
         ga.qlen = r.q->qlen;
         ga.cutoff = p->gapped_cutoff;
     }
-    PassLaunch pl{&sa, &ga, batched, scan_blocks, warps_per_block, lay.smem_bytes};
+    pl.ga = &ga;
     const bool graph = s->launch_mode == 2 || (s->launch_mode == 0 && batched);
     if ((rc = graph ? launch_pass_graph(s, pl) : launch_pass_direct(s, pl)) != BLAZE_OK) return rc;
-    s->stats.kernel_launches += 2;
+    s->stats.kernel_launches += static_cast<uint32_t>(pl.scans.size()) + 1;
     s->stats.d2h_bytes += sizeof(DevCounters);
     BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
     return BLAZE_OK;
@@ -572,39 +651,81 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
     if (n_hsps) *n_hsps = 0;
 
     constexpr size_t kSmemBudget = 220 * 1024;
-    int32_t max_qlen = 0;
-    for (uint32_t i = 0; i < nq; ++i) max_qlen = std::max(max_qlen, batched ? r.b->qlen[i] : r.q->qlen);
-    const bool qsmem = !batched && max_qlen <= kQuerySmemMax;
-    const int reg_cap = batched ? scan_batch_max_warps_by_registers() : scan_max_warps_by_registers(qsmem);
+    const int reg_cap = batched ? scan_batch_max_warps_by_registers()
+                                : scan_max_warps_by_registers(r.q->qlen <= static_cast<int32_t>(kQuerySmemMax));
     const int warp_cap = s->max_warps ? std::min(reg_cap, static_cast<int>(s->max_warps)) : reg_cap;
-    ScanLayout lay = scan_layout(max_qlen, p0->window, s->stage_bytes, kSmemBudget, warp_cap);
-    if (batched) {
-        // the batched kernel keeps every query in global memory
-        const size_t fixed = kScanMatBytes + kScanPresenceBytes;
-        lay.query_smem_bytes = 0;
-        int w = lay.warps_per_block;
-        while (w < warp_cap && fixed + static_cast<size_t>(w + 1) * lay.warp_smem_bytes <= kSmemBudget) ++w;
-        lay.warps_per_block = w;
-        lay.smem_bytes = fixed + static_cast<size_t>(w) * lay.warp_smem_bytes;
+    // layout of one scan launch for queries up to max_qlen
+    auto layout_for = [&](int32_t max_qlen) {
+        ScanLayout lay = scan_layout(max_qlen, p0->window, s->stage_bytes, kSmemBudget, warp_cap);
+        if (batched) {
+            // the batched kernel keeps every query in global memory
+            const size_t fixed = kScanMatBytes + kScanPresenceBytes;
+            lay.query_smem_bytes = 0;
+            int w = lay.warps_per_block;
+            while (w < warp_cap && fixed + static_cast<size_t>(w + 1) * lay.warp_smem_bytes <= kSmemBudget) ++w;
+            lay.warps_per_block = w;
+            lay.smem_bytes = fixed + static_cast<size_t>(w) * lay.warp_smem_bytes;
+        }
+        return lay;
+    };
+    // Length classes: a launch sizes every warp's diagonal table for its
+    // longest query, so a batch is split, shortest first, into classes whose
+    // longest query still leaves at least 4/5 of the warps per block that its
+    // shortest would get; each class is one scan launch.
+    std::vector<uint32_t> order(nq);
+    std::iota(order.begin(), order.end(), 0u);
+    if (batched)
+        std::stable_sort(order.begin(), order.end(),
+                         [&](uint32_t a, uint32_t b) { return r.b->qlen[a] < r.b->qlen[b]; });
+    auto qlen_at = [&](uint32_t k) { return batched ? r.b->qlen[order[k]] : r.q->qlen; };
+    std::vector<ScanPlan> plans;
+    for (uint32_t i = 0; i < nq;) {
+        const int base_w = layout_for(qlen_at(i)).warps_per_block;
+        uint32_t j = i + 1;
+        while (j < nq && 5 * layout_for(qlen_at(j)).warps_per_block >= 4 * base_w) ++j;
+        ScanPlan pl;
+        pl.lay = layout_for(qlen_at(j - 1));
+        pl.first = i;
+        pl.n = j - i;
+        if (pl.lay.smem_bytes > 227 * 1024) return BLAZE_ERR_LIMIT;
+        int per_sm = 0;
+        if (batched) {
+            BLAZE_CUDA_TRY(scan_batch_occupancy(pl.lay.warps_per_block, pl.lay.smem_bytes, &per_sm));
+        } else {
+            BLAZE_CUDA_TRY(scan_occupancy(pl.lay.query_smem_bytes != 0, pl.lay.warps_per_block, pl.lay.smem_bytes, &per_sm));
+        }
+        if (per_sm < 1) return BLAZE_ERR_LIMIT;
+        pl.blocks = s->n_sm * per_sm;
+        if (batched) {
+            if (s->tile_residues) {
+                pl.tile_residues = s->tile_residues;
+            } else {
+                // several tiles per warp, at most kMaxTileResidues each; a
+                // power of two so that few distinct bound tables exist
+                const uint64_t warps = static_cast<uint64_t>(pl.blocks) * pl.lay.warps_per_block;
+                const uint64_t ranges = (4 * warps + pl.n - 1) / pl.n;
+                uint64_t t = std::max<uint64_t>(db->total / std::max<uint64_t>(ranges, 1), 1);
+                t = std::min<uint64_t>(t, kMaxTileResidues);
+                uint32_t pow2 = 1;
+                while (static_cast<uint64_t>(pow2) * 2 <= t) pow2 *= 2;
+                pl.tile_residues = pow2;
+            }
+        }
+        plans.push_back(pl);
+        i = j;
     }
-    if (lay.smem_bytes > 227 * 1024) return BLAZE_ERR_LIMIT;
-    int per_sm = 0;
-    if (batched) {
-        BLAZE_CUDA_TRY(scan_batch_occupancy(lay.warps_per_block, lay.smem_bytes, &per_sm));
-    } else {
-        BLAZE_CUDA_TRY(scan_occupancy(lay.query_smem_bytes != 0, lay.warps_per_block, lay.smem_bytes, &per_sm));
-    }
-    if (per_sm < 1) return BLAZE_ERR_LIMIT;
-    const int scan_blocks = s->n_sm * per_sm;
 
     if (batched) {
-        // per-query descriptors of this run (cutoffs come from the parameters)
+        // per-query descriptors of this run in class order (cutoffs come from
+        // the parameters); the per-query arrays of the gapped stage stay in
+        // batch order
         std::vector<BatchQuery> bq(nq);
         std::vector<const uint8_t *> qp(nq);
         std::vector<int32_t> ql(nq), cut(nq);
-        for (uint32_t i = 0; i < nq; ++i) {
+        for (uint32_t k = 0; k < nq; ++k) {
+            const uint32_t i = order[k];
             const blaze_params &pi = r.p[i];
-            BatchQuery &d = bq[i];
+            BatchQuery &d = bq[k];
             d.q = r.b->d_res + r.b->res_off[i];
             d.qlen = r.b->qlen[i];
             d.ungapped_cutoff = pi.ungapped_cutoff;
@@ -614,6 +735,7 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
             d.cell_off = r.b->d_cell_off + r.b->off_off[i];
             d.diag_entries = static_cast<uint32_t>(d.qlen + pi.window + 3) & ~3u;
             d.diag_magic = static_cast<uint32_t>((1ull << 32) / d.diag_entries + 1);
+            d.index = i;
             qp[i] = d.q;
             ql[i] = d.qlen;
             cut[i] = pi.gapped_cutoff;
@@ -635,7 +757,7 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
     int rc;
     BLAZE_CUDA_TRY(cudaEventRecord(s->ev[0], s->stream));
     for (int attempt = 0;; ++attempt) {
-        if ((rc = run_pass(s, r, lay, scan_blocks)) != BLAZE_OK) return rc;
+        if ((rc = run_pass(s, r, plans)) != BLAZE_OK) return rc;
         c = *s->h_cnt;
         {
             float ms = 0.f;
@@ -802,7 +924,7 @@ extern "C" int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t) {
     if (t->launch_mode > 2) return BLAZE_ERR_INVALID_ARG;
     s->launch_mode = t->launch_mode;
     s->stage_bytes = t->stage_bytes ? t->stage_bytes : kScanStageBytes;
-    s->tile_subjects = t->tile_subjects ? t->tile_subjects : kDefaultTileSubjects;
+    s->tile_residues = t->tile_residues;
     s->max_warps = t->max_warps_per_block;
     return BLAZE_OK;
 }

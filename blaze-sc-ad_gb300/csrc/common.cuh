@@ -26,8 +26,8 @@ constexpr int kPresenceWords = (kWords + 31) / 32;                     // 686
 constexpr size_t kScanMatBytes = kAlphabet * kAlphabet;               // int8 matrix, 784
 constexpr size_t kScanPresenceBytes = (kPresenceWords * 4 + 15) & ~15; // 2752
 constexpr int32_t kQuerySmemMax = 8192;      // queries up to this length live in shared memory
-constexpr uint32_t kScanStageBytes = 2048;   // subjects up to this length are staged
-constexpr uint32_t kDefaultTileSubjects = 256;  // subjects per (query, subject range) tile of a batch
+constexpr uint32_t kScanStageBytes = 1024;   // subjects up to this length are staged
+constexpr uint32_t kMaxTileResidues = 1u << 12;  // automatic tile size at most (residues)
 
 // An ungapped HSP that reached the ungapped cutoff (NCBI BlastInitHSP analog).
 struct InitHit {
@@ -53,7 +53,6 @@ struct DevCounters {
     unsigned long long init_count;   // init hits published
     unsigned long long work_count;   // work items published
     unsigned long long out_count;    // HSPs published
-    unsigned long long next_scan;    // scan-kernel subject cursor
     unsigned long long next_gapped;  // gapped-kernel work cursor
     unsigned long long word_hits;
     unsigned long long extensions;
@@ -80,6 +79,7 @@ struct BatchQuery {
     const uint32_t *cell_start, *cell_pack, *presence;
     const uint16_t *cell_off;
     uint32_t diag_entries, diag_magic;
+    uint32_t index;  // position of the query in its batch
 };
 
 struct ScanArgs {
@@ -100,7 +100,8 @@ struct ScanArgs {
     // batched launches only
     const BatchQuery *queries;   // n_queries descriptors
     uint32_t n_queries;
-    uint32_t tile_subjects;
+    const uint32_t *tile_bounds;  // n_ranges + 1 subject indices, descending: range r is [b[r+1], b[r])
+    uint32_t n_ranges;
     uint32_t *work_query;        // query index of each work item (nullptr: one query)
     InitHit *scratch;          // per warp: scratch_cap records
     uint32_t scratch_cap;
@@ -109,6 +110,7 @@ struct ScanArgs {
     WorkItem *work;
     unsigned long long work_cap;
     DevCounters *cnt;
+    unsigned long long *cursor;  // this launch's work cursor (zeroed before the pass)
 };
 
 struct GappedArgs {

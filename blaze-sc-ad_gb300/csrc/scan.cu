@@ -498,7 +498,7 @@ scan_kernel(const ScanArgs a) {
     unsigned long long word_hits = 0, residues = 0;
     for (;;) {
         unsigned long long t = 0;
-        if (lane == 0) t = atomicAdd(&a.cnt->next_scan, 1ull);
+        if (lane == 0) t = atomicAdd(a.cursor, 1ull);
         t = __shfl_sync(kFull, t, 0);
         if (t >= a.n_subj) break;
         process_subject<QS, true>(f, a, c, q, a.n_subj - 1 - static_cast<uint32_t>(t), 0u, stage, word_hits, residues);
@@ -509,8 +509,9 @@ scan_kernel(const ScanArgs a) {
 // Many queries against the database: warps pull (query, subject range)
 // tiles; tile t covers query t mod n_queries and the (t / n_queries)-th
 // range counted from the longest subjects down, so every query's long
-// subjects come first and queries interleave. Query tables stay in global
-// memory (L1/L2 resident).
+// subjects come first and queries interleave. Ranges hold about equal
+// residues (host-computed bounds), so no tile holds up the end of the
+// launch. Query tables stay in global memory (L1/L2 resident).
 __global__ void __launch_bounds__(kScanMaxWarpsPerBlock * 32, 1)
 scan_batch_kernel(const ScanArgs a) {
     const int lane = threadIdx.x & 31;
@@ -519,12 +520,11 @@ scan_batch_kernel(const ScanArgs a) {
     uint32_t stage = 0;
     Finder f = make_finder(a, 0u, stage);
     __syncthreads();
-    const uint32_t ranges = (a.n_subj + a.tile_subjects - 1) / a.tile_subjects;
-    const unsigned long long n_tiles = static_cast<unsigned long long>(ranges) * a.n_queries;
+    const unsigned long long n_tiles = static_cast<unsigned long long>(a.n_ranges) * a.n_queries;
     unsigned long long word_hits = 0, residues = 0;
     for (;;) {
         unsigned long long t = 0;
-        if (lane == 0) t = atomicAdd(&a.cnt->next_scan, 1ull);
+        if (lane == 0) t = atomicAdd(a.cursor, 1ull);
         t = __shfl_sync(kFull, t, 0);
         if (t >= n_tiles) break;
         const uint32_t qi = static_cast<uint32_t>(t % a.n_queries);
@@ -545,10 +545,9 @@ scan_batch_kernel(const ScanArgs a) {
         Query<false> q;
         q.ptr = bq.q;
         q.len = bq.qlen;
-        const uint32_t hi = a.n_subj - range * a.tile_subjects;  // exclusive, counted from the end
-        const uint32_t lo = hi > a.tile_subjects ? hi - a.tile_subjects : 0u;
+        const uint32_t hi = a.tile_bounds[range], lo = a.tile_bounds[range + 1];
         for (uint32_t subj = hi; subj-- > lo;)
-            process_subject<false, false>(f, a, c, q, subj, qi, stage, word_hits, residues);
+            process_subject<false, false>(f, a, c, q, subj, bq.index, stage, word_hits, residues);
     }
     finish_counters(a, f, word_hits, residues);
 }

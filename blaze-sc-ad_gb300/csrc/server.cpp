@@ -116,7 +116,7 @@ void worker(blaze_server *s) {
     blaze_search *search = nullptr;
     int create_rc = blaze_search_create(s->db, &search);
     const blaze_tuning &t = s->cfg.tuning;
-    if (create_rc == BLAZE_OK && (t.stage_bytes | t.tile_subjects | t.max_warps_per_block | t.launch_mode))
+    if (create_rc == BLAZE_OK && (t.stage_bytes | t.tile_residues | t.max_warps_per_block | t.launch_mode))
         create_rc = blaze_search_set_tuning(search, &t);
     blaze_batch *b = nullptr;  // refilled for every batch: no allocation once warm
     std::vector<Request> batch;

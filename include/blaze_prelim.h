@@ -196,10 +196,12 @@ int blaze_search_batch_results(const blaze_search *s, blaze_batch_hsp *out, uint
 
 /* Launch shape of the word finder (0 = library default): subjects up to
  * stage_bytes residues are staged in shared memory; a batched tile covers
- * tile_subjects subjects; max_warps_per_block caps the block. */
+ * consecutive subjects of about tile_residues residues (a longer subject is
+ * a tile of its own; 0: sized so that every warp gets several tiles);
+ * max_warps_per_block caps the block. */
 typedef struct blaze_tuning {
     uint32_t stage_bytes;
-    uint32_t tile_subjects;
+    uint32_t tile_residues;
     uint32_t max_warps_per_block;
     /* 0: the per-pass launch sequence (counter reset, scan, gapped, counter
      * read-back) runs as a CUDA graph for batched runs and as direct launches
