@@ -20,6 +20,7 @@ fallback: without the built library or a GPU every call raises.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -57,6 +58,20 @@ class SeqSrc:
         h = ctypes.c_void_p()
         check(self._lib.blaze_db_create(int(device), u8ptr(res), u64ptr(off), off.size - 1,
                                         ctypes.byref(h)), "blaze_db_create")
+        self._adopt(h, device)
+
+    @classmethod
+    def open(cls, path: str, device: int = 0) -> "SeqSrc":
+        """An NCBI BLAST protein database volume (<path>.pin + <path>.psq)
+        loaded straight into the resident database (blaze_db_open)."""
+        self = cls.__new__(cls)
+        self._lib = load()
+        h = ctypes.c_void_p()
+        check(self._lib.blaze_db_open(int(device), os.fsencode(path), ctypes.byref(h)), "blaze_db_open")
+        self._adopt(h, device)
+        return self
+
+    def _adopt(self, h, device):
         self._h = h
         self.device = device
         tot, n, mx = ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint32()

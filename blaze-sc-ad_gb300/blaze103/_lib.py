@@ -19,7 +19,7 @@ EXPORTS = (
     "blaze_batch_create", "blaze_batch_free", "blaze_batch_info", "blaze_search_run_batch",
     "blaze_search_batch_results", "blaze_search_set_tuning",
     "blaze_server_create", "blaze_server_submit", "blaze_server_wait", "blaze_server_take",
-    "blaze_server_stats_get", "blaze_server_free",
+    "blaze_server_stats_get", "blaze_server_free", "blaze_volume_info", "blaze_volume_read", "blaze_db_open",
 )
 
 HSP_DTYPE = np.dtype([
@@ -151,6 +151,9 @@ def load(path: str | None = None):
                                     ctypes.POINTER(ctypes.c_double)]
     L.blaze_server_stats_get.argtypes = [vp, ctypes.POINTER(BlazeServerStats)]
     L.blaze_server_free.argtypes = [vp]
+    L.blaze_volume_info.argtypes = [ctypes.c_char_p, ctypes.POINTER(u32), u64p, ctypes.POINTER(u32)]
+    L.blaze_volume_read.argtypes = [ctypes.c_char_p, u8p, ctypes.c_uint64, u64p]
+    L.blaze_db_open.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.POINTER(vp)]
     for name in EXPORTS:
         if name not in ("blaze_status_string", "blaze_last_cuda_error"):
             getattr(L, name).restype = ctypes.c_int

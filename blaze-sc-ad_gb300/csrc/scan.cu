@@ -28,6 +28,7 @@ __device__ const int8_t g_blosum8[kAlphabet * kAlphabet] = {
 };
 
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kCoopSeeds = 8;  // flushes with at most this many seeds extend warp-cooperatively
 constexpr uint32_t kFlagBit = 0x80000000u;  // diagonal: an extension ran right
 constexpr uint32_t kPendBit = 0x40000000u;  // diagonal: a seed waits for its extension
 constexpr uint32_t kValMask = 0x3fffffffu;
@@ -160,6 +161,101 @@ __device__ __forceinline__ int32_t extend_two_hit(const Query<QS> &q, const Subj
 }
 
 // ------------------------------------------------------------------------
+// Warp-cooperative form of extend_two_hit for one seed: the 32 lanes take 32
+// consecutive positions of a walk per step. The running score is a prefix sum
+// and the running best a prefix maximum (carried between steps); the walk
+// stops at the first position whose stop test holds, and the best is the
+// first position reaching the final maximum -- exactly the positions and
+// scores of the sequential walk. Every lane returns the same values.
+
+// One X-drop walk of up to n positions; score and best start at `start`.
+// t(k) gives the score of the k-th position. Returns the best score; *best_k
+// is its position (-1 when never above start), *end the position the walk
+// stopped at (n when it ran out). right: also stop when the score drops to 0.
+template <bool RIGHT, typename F>
+__device__ __forceinline__ int32_t walk_warp(F t, int32_t n, int32_t start, int32_t xdrop, int32_t *best_k,
+                                             int32_t *end) {
+    const int lane = threadIdx.x & 31;
+    int32_t carry = start, cmax = start, bk = -1, stop_at = n;
+    for (int32_t base = 0; base < n; base += 32) {
+        const int32_t k = base + lane;
+        const bool valid = k < n;
+        int32_t S = valid ? t(k) : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t x = __shfl_up_sync(kFull, S, o);
+            if (lane >= o) S += x;
+        }
+        S += carry;
+        int32_t P = S;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t x = __shfl_up_sync(kFull, P, o);
+            if (lane >= o) P = max(P, x);
+        }
+        P = max(P, cmax);
+        const bool stop = valid && ((RIGHT && S <= 0) || P - S >= xdrop);
+        const unsigned sm = __ballot_sync(kFull, stop);
+        const int last = sm ? __ffs(sm) - 1 : min(31, n - 1 - base);
+        const int32_t m = __shfl_sync(kFull, P, last);
+        if (m > cmax) {
+            const unsigned hm = __ballot_sync(kFull, valid && lane <= last && S == m);
+            bk = base + __ffs(hm) - 1;
+            cmax = m;
+        }
+        carry = __shfl_sync(kFull, S, last);
+        if (sm) {
+            stop_at = base + last;
+            break;
+        }
+    }
+    *best_k = bk;
+    *end = stop_at;
+    return cmax;
+}
+
+template <bool QS, bool ST>
+__device__ __forceinline__ int32_t extend_two_hit_warp(const Query<QS> &q, const Subject<ST> &s,
+                                                       int32_t s_left_off, int32_t s_off, int32_t q_off,
+                                                       int32_t xdrop, int32_t *hsp_q, int32_t *hsp_s,
+                                                       int32_t *hsp_len, int32_t *right_extend,
+                                                       int32_t *s_last_off) {
+    int32_t score = 0, left_score = 0, right_d = 0;
+#pragma unroll
+    for (int32_t i = 0; i < kWordSize; ++i) {
+        score += score_of(q.at(q_off + i), s.at(s_off + i));
+        if (score > left_score) {
+            left_score = score;
+            right_d = i + 1;
+        }
+    }
+    const int32_t q_right = q_off + right_d, s_right = s_off + right_d;
+    // left: positions k = 0 .. min(s_right, q_right) - 1 backwards from the
+    // residue pair before (q_right, s_right)
+    int32_t bk, end;
+    left_score = walk_warp<false>(
+        [&](int32_t k) { return score_of(q.at(q_right - 1 - k), s.at(s_right - 1 - k)); },
+        min(s_right, q_right), 0, xdrop, &bk, &end);
+    const int32_t left_d = bk + 1;
+    int32_t right_score = 0, rd = 0;
+    *right_extend = 0;
+    *s_last_off = s_right;
+    if (left_d >= s_right - s_left_off) {
+        *right_extend = 1;
+        int32_t bi, iend;
+        right_score = walk_warp<true>(
+            [&](int32_t i) { return score_of(q.at(q_right + i), s.at(s_right + i)); },
+            min(s.len - s_right, q.len - q_right), left_score, xdrop, &bi, &iend);
+        rd = bi + 1;
+        *s_last_off = s_right + iend;
+    }
+    *hsp_q = q_right - left_d;
+    *hsp_s = s_right - left_d;
+    *hsp_len = left_d + rd;
+    return max(left_score, right_score);
+}
+
+// ------------------------------------------------------------------------
 // Word finder state of one warp. The diagonal table holds, per diagonal
 // (s - q) mod L, either the last recorded hit (biased by window and by a
 // running base so the table never needs clearing between subjects), the same
@@ -257,7 +353,31 @@ __device__ void flush(Finder &f, const ScanArgs &a, const Ctx &c, const Query<QS
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
     while (f.n_seed > 0 || f.n_defer > 0) {
-        for (int c0 = 0; c0 < f.n_seed; c0 += 32) {
+        // few seeds: one at a time with the whole warp on each walk
+        for (int i = 0; f.n_seed <= kCoopSeeds && i < f.n_seed; ++i) {
+            const int4 sd = get_seed(f, i);
+            int32_t hq, hs, hl, rext, slast;
+            const int32_t score =
+                extend_two_hit_warp(q, sub, sd.z, sd.y, sd.x, c.xdrop, &hq, &hs, &hl, &rext, &slast);
+            if (lane == 0) {
+                sts32(f.diag + 4u * static_cast<uint32_t>(sd.w),
+                      rext ? (kFlagBit | (static_cast<uint32_t>(slast - (kWordSize - 1) + c.window) + f.base))
+                           : (static_cast<uint32_t>(sd.y + c.window) + f.base));
+                if (score >= c.cutoff && f.n_init < a.scratch_cap) {
+                    InitHit h;
+                    h.q_start = hq;
+                    h.s_start = hs;
+                    h.len = hl;
+                    h.score = score;
+                    h.q_trig = sd.x;
+                    h.s_trig = sd.y;
+                    f.scratch[f.n_init] = h;
+                }
+            }
+            if (score >= c.cutoff) ++f.n_init;
+        }
+        // many: one lane per seed
+        for (int c0 = 0; f.n_seed > kCoopSeeds && c0 < f.n_seed; c0 += 32) {
             const int i = c0 + lane;
             bool pass = false;
             int32_t hq = 0, hs = 0, hl = 0, score = 0;

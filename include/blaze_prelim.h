@@ -127,6 +127,20 @@ int blaze_db_free(blaze_db *db);
 int blaze_db_info(const blaze_db *db, uint64_t *total_residues, uint32_t *n_subjects,
                   uint32_t *max_length);
 
+/* NCBI BLAST protein database volume: `path` without extension names the
+ * <path>.pin index and <path>.psq sequence file (format versions 4 and 5).
+ * OID i of the volume becomes subject i. Replaces the per-subject
+ * BlastSeqSrcGetSequence gathers of the reference's GPU driver
+ * (BLAZE_gpu/gpuBLAZE.cu:1587-1611). Malformed or non-protein volumes return
+ * BLAZE_ERR_INVALID_ARG. */
+int blaze_volume_info(const char *path, uint32_t *n_subjects, uint64_t *total_residues,
+                      uint32_t *max_length);
+/* Residues of every sequence, concatenated without separators, and n+1
+ * offsets (capacity: residues bytes available). */
+int blaze_volume_read(const char *path, uint8_t *residues, uint64_t capacity, uint64_t *offsets);
+/* blaze_volume_read + blaze_db_create. */
+int blaze_db_open(int device, const char *path, blaze_db **out);
+
 /* Query: NCBIstdaa codes 1..27, 1 <= length <= 32000. Builds the word lookup
  * (every word scoring >= word_threshold against a query word, plus the query
  * word itself) and uploads it. */
