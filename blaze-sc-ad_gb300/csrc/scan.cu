@@ -28,7 +28,7 @@ __device__ const int8_t g_blosum8[kAlphabet * kAlphabet] = {
 };
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kCoopSeeds = 8;  // flushes with at most this many seeds extend warp-cooperatively
+constexpr int kCoopSeeds = 4;  // flushes with at most this many seeds extend warp-cooperatively
 constexpr uint32_t kFlagBit = 0x80000000u;  // diagonal: an extension ran right
 constexpr uint32_t kPendBit = 0x40000000u;  // diagonal: a seed waits for its extension
 constexpr uint32_t kValMask = 0x3fffffffu;
