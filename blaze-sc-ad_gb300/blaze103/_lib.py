@@ -45,6 +45,7 @@ class BlazeParams(ctypes.Structure):
         ("gapped_xdrop", ctypes.c_int32), ("gapped_cutoff", ctypes.c_int32),
         ("lambda_", ctypes.c_double), ("K", ctypes.c_double),
         ("eff_searchsp", ctypes.c_double), ("prelim_evalue", ctypes.c_double),
+        ("hitlist_size", ctypes.c_int32), ("max_hsps", ctypes.c_int32),
     ]
 
     def as_dict(self) -> dict:

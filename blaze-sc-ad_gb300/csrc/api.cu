@@ -822,13 +822,18 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
     std::sort(groups.begin(), groups.end(), [](const Group &a, const Group &b) {
         return a.query != b.query ? a.query < b.query : a.oid < b.oid;
     });
-    if (batched) s->batch_results.reserve(n_out);
-    else s->results.reserve(n_out);
-    uint32_t subjects = 0;
+    // E-values, the preliminary reap and per-subject max_hsps, then per query
+    // the hitlist_size subjects with the best E-values (a subject's best is
+    // its first HSP; ties by smaller OID), emitted in OID order
+    struct Kept { uint32_t query, oid; int32_t best; size_t first, n; };
+    std::vector<blaze_hsp> kept_hsps;
+    kept_hsps.reserve(n_out);
+    std::vector<Kept> kept;
     for (const Group &g : groups) {
         const blaze_params &pg = r.p[g.query];
-        size_t kept = 0;
+        const size_t first = kept_hsps.size();
         for (size_t k = 0; k < g.n; ++k) {
+            if (pg.max_hsps > 0 && kept_hsps.size() - first >= static_cast<size_t>(pg.max_hsps)) break;
             const DevHsp &d = s->h_out[g.first + k];
             blaze_hsp h;
             h.oid = g.oid;
@@ -841,18 +846,45 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
             h.s_gapped_start = d.s_gs;
             h.evalue = pg.eff_searchsp * pg.K * std::exp(-pg.lambda * static_cast<double>(d.score));
             if (h.evalue > pg.prelim_evalue) continue;  // preliminary E-value reap
+            kept_hsps.push_back(h);
+        }
+        if (kept_hsps.size() > first)
+            kept.push_back({g.query, g.oid, kept_hsps[first].score, first, kept_hsps.size() - first});
+    }
+    for (size_t i = 0; i < kept.size();) {  // hitlist per query
+        size_t j = i;
+        while (j < kept.size() && kept[j].query == kept[i].query) ++j;
+        const int32_t limit = r.p[kept[i].query].hitlist_size;
+        if (limit > 0 && j - i > static_cast<size_t>(limit)) {
+            std::vector<Kept> by_best(kept.begin() + i, kept.begin() + j);
+            std::sort(by_best.begin(), by_best.end(), [](const Kept &a, const Kept &b) {
+                return a.best != b.best ? a.best > b.best : a.oid < b.oid;
+            });
+            const Kept &cut = by_best[static_cast<size_t>(limit) - 1];
+            for (size_t k = i; k < j; ++k) {  // keep those ranked at or above the cut
+                const bool above = kept[k].best > cut.best || (kept[k].best == cut.best && kept[k].oid <= cut.oid);
+                if (!above) kept[k].n = 0;
+            }
+        }
+        i = j;
+    }
+    if (batched) s->batch_results.reserve(kept_hsps.size());
+    else s->results.reserve(kept_hsps.size());
+    uint32_t subjects = 0;
+    for (const Kept &k : kept) {
+        if (k.n == 0) continue;
+        ++subjects;
+        for (size_t t = 0; t < k.n; ++t) {
             if (batched) {
                 blaze_batch_hsp bh;
-                bh.query = g.query;
+                bh.query = k.query;
                 bh.reserved = 0;
-                bh.hsp = h;
+                bh.hsp = kept_hsps[k.first + t];
                 s->batch_results.push_back(bh);
             } else {
-                s->results.push_back(h);
+                s->results.push_back(kept_hsps[k.first + t]);
             }
-            ++kept;
         }
-        subjects += kept > 0;
     }
     const size_t n_res = batched ? s->batch_results.size() : s->results.size();
     s->last_init_count = c.init_count;

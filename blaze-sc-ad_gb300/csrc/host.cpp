@@ -163,6 +163,8 @@ int default_params(int32_t qlen, uint64_t db_len, uint32_t db_n, double evalue, 
         (kGapTriggerBits * kLn2 + std::log(kUngappedK)) / kUngappedLambda);
     p->ungapped_cutoff = std::min(gap_trigger, p->gapped_cutoff);
     p->prelim_evalue = evalue;
+    p->hitlist_size = 0;
+    p->max_hsps = 0;
     return BLAZE_OK;
 }
 

@@ -65,6 +65,11 @@ typedef struct blaze_params {
     double K;                /* gapped Karlin-Altschul K */
     double eff_searchsp;     /* effective search space of the query */
     double prelim_evalue;    /* HSPs with a larger E-value are dropped */
+    /* Culling of the returned lists (0: none). hitlist_size (NCBI
+     * max_target_seqs): per query, the subjects with the best E-values, ties
+     * by smaller OID. max_hsps: per subject, the first HSPs of its list. */
+    int32_t hitlist_size;
+    int32_t max_hsps;
 } blaze_params;
 
 /* One HSP of a subject; offsets 0-based, ends exclusive (NCBI BlastHSP's

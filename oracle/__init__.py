@@ -177,7 +177,7 @@ def default_params(qlen: int, db_len: int, db_n: int, evalue: float = 10.0) -> d
                 ungapped_cutoff=min(gap_trigger, gapped_cutoff), gap_open=11, gap_extend=1,
                 gapped_xdrop=int(15.0 * ln2 / g["lam"]), gapped_cutoff=gapped_cutoff,
                 lam=g["lam"], K=g["K"], eff_searchsp=float(searchsp), prelim_evalue=evalue,
-                length_adjustment=ell)
+                hitlist_size=0, max_hsps=0, length_adjustment=ell)
 
 
 def finish(hsps: np.ndarray, params) -> np.ndarray:
@@ -192,4 +192,30 @@ def finish(hsps: np.ndarray, params) -> np.ndarray:
     for n in HSP_DTYPE.names:
         out[n] = hsps[n]
     out["evalue"] = ev
-    return out[ev <= cut]
+    out = out[ev <= cut]
+    return cull(out, get("hitlist_size") if _has(params, "hitlist_size") else 0,
+                get("max_hsps") if _has(params, "max_hsps") else 0)
+
+
+def _has(params, key) -> bool:
+    return key in params if isinstance(params, dict) else hasattr(params, key)
+
+
+def cull(hsps: np.ndarray, hitlist_size: int = 0, max_hsps: int = 0) -> np.ndarray:
+    """max_hsps: the first HSPs of each subject's list; hitlist_size: the
+    subjects with the best E-values (their first HSP), ties by smaller
+    subject index. Plain loops: test sizes only."""
+    if max_hsps > 0:
+        keep, seen = [], {}
+        for i, sub in enumerate(hsps["subject"].tolist()):
+            seen[sub] = seen.get(sub, 0) + 1
+            if seen[sub] <= max_hsps:
+                keep.append(i)
+        hsps = hsps[np.array(keep, dtype=np.int64)]
+    if hitlist_size > 0:
+        best = {}
+        for sub, sc in zip(hsps["subject"].tolist(), hsps["score"].tolist()):
+            best.setdefault(sub, sc)  # first HSP of each subject
+        ranked = sorted(best, key=lambda sub: (-best[sub], sub))[:hitlist_size]
+        hsps = hsps[np.isin(hsps["subject"], np.array(ranked, dtype=hsps["subject"].dtype))]
+    return hsps

@@ -143,3 +143,25 @@ def test_query_longer_than_shared_copy():
     res, off = concat(seqs)
     got, _, _ = compare(q, res, off)
     assert len(got) > 10
+
+
+@pytest.mark.parametrize("cull", [dict(hitlist_size=7), dict(max_hsps=1), dict(hitlist_size=3, max_hsps=2),
+                                  dict(hitlist_size=100000)])
+def test_hitlist_culling(cull):
+    rng = np.random.default_rng(77)
+    q = synth.random_residues(rng, 400)
+    seqs = [synth.random_residues(rng, int(L)) for L in synth.lognormal_lengths(rng, 600, 250, 0.82, 30, 3000)]
+    for i in range(0, len(seqs), 3):  # many hits, several HSPs per subject
+        for _ in range(2):
+            s0 = int(rng.integers(0, len(q) - 120))
+            hom = synth.mutate(rng, q[s0:s0 + 120], 0.5)
+            pos = int(rng.integers(0, len(seqs[i]) + 1))
+            seqs[i] = np.concatenate([seqs[i][:pos], hom, seqs[i][pos:]])
+    res, off = concat(seqs)
+    got, ref, _ = compare(q, res, off, **cull)
+    full, _, _ = compare(q, res, off)
+    assert len(got) > 0
+    if "hitlist_size" in cull:
+        assert len(set(got["oid"].tolist())) == min(cull["hitlist_size"], len(set(full["oid"].tolist())))
+    if "max_hsps" in cull:
+        assert np.bincount(got["oid"]).max() <= cull["max_hsps"]
