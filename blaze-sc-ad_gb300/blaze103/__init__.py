@@ -25,11 +25,11 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import (BATCH_HSP_DTYPE, HSP_DTYPE, INIT_DTYPE, BlazeError, BlazeParams, BlazeServerConfig,
+from ._lib import (ALIGNED_DTYPE, BATCH_HSP_DTYPE, HSP_DTYPE, INIT_DTYPE, BlazeError, BlazeParams, BlazeServerConfig,
                    BlazeServerStats, BlazeStats, BlazeTuning, check, load, u8ptr, u64ptr, status_string)
 
 __all__ = ["SeqSrc", "PrelimSearch", "HSPResults", "QueryBatch", "Server", "BlazeParams", "BlazeTuning",
-           "BlazeError", "HSP_DTYPE", "BATCH_HSP_DTYPE", "default_params", "device_count", "load",
+           "BlazeError", "HSP_DTYPE", "BATCH_HSP_DTYPE", "ALIGNED_DTYPE", "default_params", "device_count", "load",
            "status_string"]
 
 
@@ -284,6 +284,25 @@ class PrelimSearch:
                                                    n.value, ctypes.byref(n)),
               "blaze_search_batch_results")
         return out
+
+    def traceback(self, query, params: BlazeParams, evalue: float | None = None,
+                  final_xdrop: int = 64) -> np.ndarray:
+        """Traceback stage over the last single-query run (which must have
+        searched `query` with `params`): ALIGNED_DTYPE records by OID, then
+        the final per-subject order, reaped at `evalue` (default: the
+        preliminary E-value)."""
+        q = Query(self.seq_src, query, params.word_threshold)
+        try:
+            n = ctypes.c_uint64()
+            ev = params.prelim_evalue if evalue is None else float(evalue)
+            check(self._lib.blaze_search_traceback(self._h, q.handle, ctypes.byref(params), int(final_xdrop), ev,
+                                                   ctypes.byref(n)), "blaze_search_traceback")
+            out = np.zeros(n.value, dtype=ALIGNED_DTYPE)
+            check(self._lib.blaze_search_traceback_results(self._h, out.ctypes.data_as(ctypes.c_void_p), n.value,
+                                                           ctypes.byref(n)), "blaze_search_traceback_results")
+            return out[: n.value]
+        finally:
+            q.close()
 
     def prelim_search(self, query, params: BlazeParams, capacity: int) -> np.ndarray:
         """The one-call C-ABI path with host buffers (blaze_prelim_search)."""

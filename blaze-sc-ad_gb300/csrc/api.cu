@@ -36,6 +36,7 @@ struct blaze_db {
     uint32_t n = 0;
     uint32_t max_len = 0;
     std::vector<uint32_t> oid_of;  // sorted index -> OID
+    std::vector<uint32_t> sorted_of;  // OID -> sorted index
     std::vector<uint64_t> h_off;   // offsets of the length-sorted copy (host)
 };
 
@@ -115,6 +116,14 @@ struct blaze_search {
     uint32_t *h_outq = nullptr;  // pinned
     size_t h_outq_n = 0;
     std::vector<blaze_batch_hsp> batch_results;
+    // traceback stage
+    DevBuf<TbItem> tb_items;
+    DevBuf<TbOut> tb_out;
+    DevBuf<uint8_t> tb_dirs;
+    DevBuf<int32_t> tb_rows, tb_dp;
+    DevBuf<unsigned long long> tb_cursor;
+    unsigned long long tb_dir_cap = 1ull << 18;  // direction bytes per warp; doubles on overflow
+    std::vector<blaze_aligned_hsp> tb_results;
 };
 
 struct blaze_batch {
@@ -179,6 +188,8 @@ extern "C" int blaze_db_create(int device, const uint8_t *residues, const uint64
     for (uint32_t i = 1; i < n_subjects && sorted; ++i) sorted = len(i - 1) <= len(i);
     if (!sorted) std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return len(a) < len(b); });
     db->oid_of = order;
+    db->sorted_of.resize(n_subjects);
+    for (uint32_t k = 0; k < n_subjects; ++k) db->sorted_of[order[k]] = k;
     std::vector<uint64_t> off(n_subjects + 1);
     off[0] = 0;
     for (uint32_t k = 0; k < n_subjects; ++k) {
@@ -323,6 +334,7 @@ extern "C" int blaze_search_create(blaze_db *db, blaze_search **out) {
     if (const char *v = std::getenv("BLAZE_INITIAL_INIT_CAP")) s->init_cap = std::max(1, std::atoi(v));
     if (const char *v = std::getenv("BLAZE_INITIAL_OUT_CAP")) s->out_cap = std::max(1, std::atoi(v));
     if (const char *v = std::getenv("BLAZE_INITIAL_WORK_CAP")) s->work_cap = std::max(1, std::atoi(v));
+    if (const char *v = std::getenv("BLAZE_INITIAL_TRACEBACK_CAP")) s->tb_dir_cap = std::max(64, std::atoi(v));
     *out = s;
     return BLAZE_OK;
 }
@@ -347,6 +359,12 @@ extern "C" int blaze_search_free(blaze_search *s) {
     s->work_query.release();
     s->out_query.release();
     s->cursors.release();
+    s->tb_items.release();
+    s->tb_out.release();
+    s->tb_dirs.release();
+    s->tb_rows.release();
+    s->tb_dp.release();
+    s->tb_cursor.release();
     if (s->h_outq) cudaFreeHost(s->h_outq);
     if (s->d_cnt) cudaFree(s->d_cnt);
     if (s->h_cnt) cudaFreeHost(s->h_cnt);
@@ -1169,4 +1187,149 @@ extern "C" int blaze_prelim_search(blaze_search *s, const uint8_t *query, int32_
     blaze_query_free(q);
     if (rc != BLAZE_OK) return rc;
     return blaze_search_results(s, out, capacity, n_hsps);
+}
+
+// ------------------------------------------------------------------------
+// Traceback stage.
+
+extern "C" int blaze_search_traceback(blaze_search *s, const blaze_query *q, const blaze_params *p,
+                                      int32_t final_xdrop, double evalue, uint64_t *n_hsps) {
+    if (!s || !q || !p || final_xdrop <= 0 || q->device != s->db->device || s->last_batched)
+        return BLAZE_ERR_INVALID_ARG;
+    int rc = check_params(p);
+    if (rc != BLAZE_OK) return rc;
+    if (n_hsps) *n_hsps = 0;
+    s->tb_results.clear();
+    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
+    const blaze_db *db = s->db;
+    const size_t n = s->results.size();
+    std::vector<TbItem> items(n);
+    for (size_t i = 0; i < n; ++i) {
+        const blaze_hsp &h = s->results[i];
+        if (h.oid >= db->n || h.q_gapped_start < 0 || h.q_gapped_start >= q->qlen) return BLAZE_ERR_INVALID_ARG;
+        const uint32_t sub = db->sorted_of[h.oid];
+        if (h.s_gapped_start < 0 || static_cast<uint64_t>(h.s_gapped_start) >= db->h_off[sub + 1] - db->h_off[sub])
+            return BLAZE_ERR_INVALID_ARG;
+        items[i] = TbItem{sub, h.q_gapped_start, h.s_gapped_start, 0u};
+    }
+    std::vector<TbOut> outs(n);
+    if (n > 0) {
+        const int blocks = s->n_sm;
+        const size_t warps = static_cast<size_t>(blocks) * kTracebackWarpsPerBlock;
+        const uint32_t row_cap = static_cast<uint32_t>(q->qlen) + 2u;
+        const uint32_t dp_stride = std::max<uint32_t>(db->max_len, 1u) + 2u;
+        if ((rc = s->tb_items.ensure(n)) != BLAZE_OK) return rc;
+        if ((rc = s->tb_out.ensure(n)) != BLAZE_OK) return rc;
+        if ((rc = s->tb_rows.ensure(warps * 3 * row_cap)) != BLAZE_OK) return rc;
+        if ((rc = s->tb_dp.ensure(warps * 2 * dp_stride)) != BLAZE_OK) return rc;
+        if ((rc = s->tb_cursor.ensure(1)) != BLAZE_OK) return rc;
+        BLAZE_CUDA_TRY(cudaMemcpyAsync(s->tb_items.p, items.data(), sizeof(TbItem) * n, cudaMemcpyHostToDevice,
+                                       s->stream));
+        s->stats.h2d_bytes += sizeof(TbItem) * n;
+        for (int attempt = 0;; ++attempt) {
+            if ((rc = s->tb_dirs.ensure(warps * s->tb_dir_cap)) != BLAZE_OK) return rc;
+            TracebackArgs ta{};
+            ta.res = db->d_res;
+            ta.off = db->d_off;
+            ta.q = q->d_q;
+            ta.qlen = q->qlen;
+            ta.items = s->tb_items.p;
+            ta.n_items = static_cast<uint32_t>(n);
+            ta.out = s->tb_out.p;
+            ta.gap_open = p->gap_open;
+            ta.gap_extend = p->gap_extend;
+            ta.xdrop = final_xdrop;
+            ta.dp = s->tb_dp.p;
+            ta.dp_stride = dp_stride;
+            ta.dirs = s->tb_dirs.p;
+            ta.dir_cap = s->tb_dir_cap;
+            ta.rows = s->tb_rows.p;
+            ta.row_cap = row_cap;
+            ta.cursor = s->tb_cursor.p;
+            BLAZE_CUDA_TRY(cudaMemsetAsync(s->tb_cursor.p, 0, sizeof(unsigned long long), s->stream));
+            BLAZE_CUDA_TRY(launch_traceback(ta, blocks, s->stream));
+            s->stats.kernel_launches += 1;
+            BLAZE_CUDA_TRY(cudaMemcpyAsync(outs.data(), s->tb_out.p, sizeof(TbOut) * n, cudaMemcpyDeviceToHost,
+                                           s->stream));
+            BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
+            s->stats.d2h_bytes += sizeof(TbOut) * n;
+            bool overflow = false;
+            for (const TbOut &o : outs) {
+                if (o.status == 2) return BLAZE_ERR_INTERNAL;
+                overflow |= o.status == 1;
+            }
+            if (!overflow) break;
+            if (attempt >= 20) return BLAZE_ERR_LIMIT;
+            s->tb_dir_cap *= 2;  // a longer alignment than the buffers held: again, larger
+        }
+    }
+    // per subject: purge shared end points, order, E-values, reap
+    const double ln2 = std::log(2.0), lnK = std::log(p->K);
+    for (size_t i = 0; i < n;) {
+        size_t j = i;
+        while (j < n && s->results[j].oid == s->results[i].oid) ++j;
+        std::vector<TbOut> g(outs.begin() + i, outs.begin() + j);
+        auto by_start = [](const TbOut &a, const TbOut &b) {
+            if (a.q_start != b.q_start) return a.q_start < b.q_start;
+            if (a.s_start != b.s_start) return a.s_start < b.s_start;
+            if (a.score != b.score) return a.score > b.score;
+            if (a.q_end != b.q_end) return a.q_end > b.q_end;
+            return a.s_end > b.s_end;
+        };
+        auto by_end = [](const TbOut &a, const TbOut &b) {
+            if (a.q_end != b.q_end) return a.q_end < b.q_end;
+            if (a.s_end != b.s_end) return a.s_end < b.s_end;
+            if (a.score != b.score) return a.score > b.score;
+            if (a.q_start != b.q_start) return a.q_start < b.q_start;
+            return a.s_start < b.s_start;
+        };
+        auto by_score = [](const TbOut &a, const TbOut &b) {
+            if (a.score != b.score) return a.score > b.score;
+            if (a.s_start != b.s_start) return a.s_start < b.s_start;
+            if (a.s_end != b.s_end) return a.s_end > b.s_end;
+            if (a.q_start != b.q_start) return a.q_start < b.q_start;
+            return a.q_end > b.q_end;
+        };
+        std::stable_sort(g.begin(), g.end(), by_start);
+        std::vector<TbOut> m;
+        for (const TbOut &o : g)
+            if (m.empty() || o.q_start != m.back().q_start || o.s_start != m.back().s_start) m.push_back(o);
+        std::stable_sort(m.begin(), m.end(), by_end);
+        std::vector<TbOut> m2;
+        for (const TbOut &o : m)
+            if (m2.empty() || o.q_end != m2.back().q_end || o.s_end != m2.back().s_end) m2.push_back(o);
+        std::stable_sort(m2.begin(), m2.end(), by_score);
+        for (const TbOut &o : m2) {
+            blaze_aligned_hsp h{};
+            h.oid = s->results[i].oid;
+            h.score = o.score;
+            h.q_start = o.q_start;
+            h.q_end = o.q_end;
+            h.s_start = o.s_start;
+            h.s_end = o.s_end;
+            h.length = o.length;
+            h.identities = o.identities;
+            h.positives = o.positives;
+            h.mismatches = o.mismatches;
+            h.gap_opens = o.gap_opens;
+            h.gaps = o.gaps;
+            h.evalue = p->eff_searchsp * p->K * std::exp(-p->lambda * static_cast<double>(o.score));
+            h.bit_score = (p->lambda * static_cast<double>(o.score) - lnK) / ln2;
+            if (h.evalue <= evalue) s->tb_results.push_back(h);
+        }
+        i = j;
+    }
+    if (n_hsps) *n_hsps = s->tb_results.size();
+    return BLAZE_OK;
+}
+
+extern "C" int blaze_search_traceback_results(const blaze_search *s, blaze_aligned_hsp *out, uint64_t capacity,
+                                              uint64_t *n_hsps) {
+    if (!s) return BLAZE_ERR_INVALID_ARG;
+    const size_t n = s->tb_results.size();
+    if (n_hsps) *n_hsps = n;
+    if (capacity < n) return BLAZE_ERR_OUTPUT_TOO_SMALL;
+    if (n && !out) return BLAZE_ERR_INVALID_ARG;
+    if (n) std::memcpy(out, s->tb_results.data(), sizeof(blaze_aligned_hsp) * n);
+    return BLAZE_OK;
 }

@@ -145,12 +145,45 @@ struct ScanLayout {
     size_t smem_bytes;
 };
 
-// Launchers (scan.cu, kernels.cu).
+// Traceback stage: one preliminary HSP to trace from its gapped start point.
+struct TbItem {
+    uint32_t subject;  // index into the length-sorted database
+    int32_t q_off, s_off;
+    uint32_t pad;
+};
+
+struct TbOut {
+    int32_t score, q_start, q_end, s_start, s_end;
+    int32_t length, identities, positives, mismatches, gap_opens, gaps;
+    int32_t status;  // 0 done, 1 direction buffer too small, 2 inconsistent path
+};
+
+struct TracebackArgs {
+    const uint8_t *res;
+    const uint64_t *off;
+    const uint8_t *q;
+    int32_t qlen;
+    const TbItem *items;
+    uint32_t n_items;
+    TbOut *out;
+    int32_t gap_open, gap_extend, xdrop;
+    int32_t *dp;                // per warp: H and E rows of dp_stride ints each
+    uint32_t dp_stride;
+    uint8_t *dirs;              // per warp: dir_cap direction bytes
+    unsigned long long dir_cap;
+    int32_t *rows;              // per warp: 3 ints (first, end, offset) per DP row
+    uint32_t row_cap;
+    unsigned long long *cursor;
+};
+
+// Launchers (scan.cu, kernels.cu, traceback.cu).
 ScanLayout scan_layout(int32_t qlen, int32_t window, uint32_t stage_bytes, size_t smem_budget, int max_warps);
 cudaError_t launch_scan(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem, cudaStream_t st);
 cudaError_t scan_occupancy(bool query_in_smem, int warps_per_block, size_t smem, int *blocks_per_sm);
 int scan_max_warps_by_registers(bool query_in_smem);
 cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st);
+constexpr int kTracebackWarpsPerBlock = 4;
+cudaError_t launch_traceback(const TracebackArgs &a, int n_blocks, cudaStream_t st);
 cudaError_t launch_scan_batch(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem, cudaStream_t st);
 cudaError_t scan_batch_occupancy(int warps_per_block, size_t smem, int *blocks_per_sm);
 int scan_batch_max_warps_by_registers();

@@ -181,6 +181,30 @@ int blaze_search_init_hits(blaze_search *s, blaze_init_hit *out, uint64_t capaci
                            uint64_t *n_hits);
 
 /* ---------------------------------------------------------------------
+ * Traceback stage (after the preliminary search; NCBI's traceback of
+ * BLAZE_ncbi/prelim_stage.cpp:1462-1498): every HSP of the last single-query
+ * run of s is aligned again from its gapped start point with the final
+ * X-drop (NCBI blastp: 64 = 25 bits), keeping the path; per subject,
+ * duplicates are purged and the list sorted as in the preliminary stage;
+ * E-values come from the final scores and HSPs above `evalue` are dropped.
+ * q must hold the query of that run. */
+typedef struct blaze_aligned_hsp {
+    uint32_t oid;
+    int32_t score;
+    int32_t q_start, q_end, s_start, s_end; /* 0-based, ends exclusive */
+    int32_t length;                         /* aligned columns */
+    int32_t identities, positives, mismatches, gap_opens, gaps;
+    int32_t reserved;
+    double evalue;
+    double bit_score;                       /* (lambda * score - ln K) / ln 2 */
+} blaze_aligned_hsp;
+int blaze_search_traceback(blaze_search *s, const blaze_query *q, const blaze_params *params, int32_t final_xdrop,
+                           double evalue, uint64_t *n_hsps);
+/* Results of the last traceback, by OID, then the final per-subject order. */
+int blaze_search_traceback_results(const blaze_search *s, blaze_aligned_hsp *out, uint64_t capacity,
+                                   uint64_t *n_hsps);
+
+/* ---------------------------------------------------------------------
  * Batched form: many queries of uneven length against the database in one
  * persistent launch per stage. Warps pull (query, subject range) tiles from a
  * device work queue, longest subjects first, queries interleaved. All

@@ -74,6 +74,12 @@ def lib():
         L.orc_semi_gapped.argtypes = [u8p, u8p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                       ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, i32p, i32p]
         L.orc_semi_gapped.restype = ctypes.c_int32
+        L.orc_traceback.argtypes = [u8p, ctypes.c_int32, u8p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                    ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(OrcTb)]
+        L.orc_traceback.restype = ctypes.c_int
+        L.orc_traceback_ops.argtypes = L.orc_traceback.argtypes + [ctypes.c_char_p, ctypes.c_int32,
+                                                                   ctypes.POINTER(ctypes.c_int32)]
+        L.orc_traceback_ops.restype = ctypes.c_int
         L.orc_gapped_start.argtypes = [u8p, u8p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
         L.orc_gapped_start.restype = ctypes.c_int32
         L.orc_evalue.argtypes = [ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double]
@@ -141,6 +147,93 @@ def semi_gapped(A, B, M, N, reverse, gap_open=11, gap_extend=1, xdrop=38):
     s = lib().orc_semi_gapped(ap, bp, M, N, int(reverse), gap_open, gap_extend, xdrop,
                               ctypes.byref(ab), ctypes.byref(bb))
     return s, ab.value, bb.value
+
+
+class OrcTb(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "score", "q_start", "q_end", "s_start", "s_end", "length", "identities", "positives", "mismatches",
+        "gap_opens", "gaps")]
+
+
+TB_FIELDS = [n for n, _ in OrcTb._fields_]
+FINAL_XDROP = 64  # NCBI blastp gap_x_dropoff_final: 25 bits at lambda 0.267
+
+
+def traceback(query, subject, q_off, s_off, gap_open=11, gap_extend=1, xdrop=FINAL_XDROP) -> dict:
+    """Traceback of one HSP from its gapped start point (orc_traceback)."""
+    q, qp = _u8(query if len(query) else [0])
+    t, tp = _u8(subject if len(subject) else [0])
+    out = OrcTb()
+    rc = lib().orc_traceback(qp, len(query), tp, len(subject), int(q_off), int(s_off), gap_open, gap_extend,
+                             xdrop, ctypes.byref(out))
+    if rc != 0:
+        raise RuntimeError("oracle traceback failed")
+    return {n: getattr(out, n) for n in TB_FIELDS}
+
+
+def traceback_ops(query, subject, q_off, s_off, gap_open=11, gap_extend=1, xdrop=FINAL_XDROP):
+    """(stats, moves) of one traceback; moves in query order as 'M'/'I'/'D'."""
+    q, qp = _u8(query if len(query) else [0])
+    t, tp = _u8(subject if len(subject) else [0])
+    out = OrcTb()
+    cap = 2 * (len(query) + len(subject)) + 8
+    buf = ctypes.create_string_buffer(cap)
+    n = ctypes.c_int32()
+    rc = lib().orc_traceback_ops(qp, len(query), tp, len(subject), int(q_off), int(s_off), gap_open, gap_extend,
+                                 xdrop, ctypes.byref(out), buf, cap, ctypes.byref(n))
+    if rc != 0:
+        raise RuntimeError("oracle traceback failed")
+    return {n_: getattr(out, n_) for n_ in TB_FIELDS}, buf.raw[: n.value].decode()
+
+
+def traceback_hsps(query, residues, offsets, hsps, params, xdrop=FINAL_XDROP, evalue=None) -> list:
+    """The traceback stage over a preliminary result (records with
+    'subject', 'q_gstart', 's_gstart'): every HSP traced from its start
+    point, then per subject duplicates purged and the list sorted as in the
+    preliminary stage, E-values from the final scores and the reap at
+    `evalue` (default: the parameters' preliminary E-value). Returns dicts
+    with 'subject' and 'evalue' added, by subject then final order."""
+    get = (lambda k: params[k]) if isinstance(params, dict) else (lambda k: getattr(params, k))
+    lam = get("lam") if isinstance(params, dict) else params.lambda_
+    K, ss = get("K"), get("eff_searchsp")
+    cut = get("prelim_evalue") if evalue is None else evalue
+    out = []
+    subs = hsps["subject"].tolist()
+    i = 0
+    while i < len(subs):
+        j = i
+        while j < len(subs) and subs[j] == subs[i]:
+            j += 1
+        sub = subs[i]
+        S = residues[int(offsets[sub]):int(offsets[sub + 1])]
+        traced = []
+        for k in range(i, j):
+            r = traceback(query, S, int(hsps["q_gstart"][k]), int(hsps["s_gstart"][k]), get("gap_open"),
+                          get("gap_extend"), xdrop)
+            r["subject"] = sub
+            traced.append(r)
+        kept = _purge_and_sort(traced)
+        for r in kept:
+            r["evalue"] = ss * K * float(np.exp(-lam * r["score"]))
+            if r["evalue"] <= cut:
+                out.append(r)
+        i = j
+    return out
+
+
+def _purge_and_sort(hs: list) -> list:
+    """Same rules as the preliminary stage's purge and final order."""
+    by_start = sorted(hs, key=lambda h: (h["q_start"], h["s_start"], -h["score"], -h["q_end"], -h["s_end"]))
+    m = []
+    for h in by_start:
+        if not m or h["q_start"] != m[-1]["q_start"] or h["s_start"] != m[-1]["s_start"]:
+            m.append(h)
+    by_end = sorted(m, key=lambda h: (h["q_end"], h["s_end"], -h["score"], h["q_start"], h["s_start"]))
+    m = []
+    for h in by_end:
+        if not m or h["q_end"] != m[-1]["q_end"] or h["s_end"] != m[-1]["s_end"]:
+            m.append(h)
+    return sorted(m, key=lambda h: (-h["score"], h["s_start"], -h["s_end"], h["q_start"], -h["q_end"]))
 
 
 def gapped_start(q, s, q_start, s_start, length):

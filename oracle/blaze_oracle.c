@@ -389,6 +389,264 @@ int32_t orc_semi_gapped(const uint8_t *A, const uint8_t *B, int32_t M, int32_t N
     return r;
 }
 
+/* ------------------------------------------------------------- traceback */
+
+/* Direction byte of a DP cell: bits 0-1 where H came from (0 diagonal, 1
+ * vertical gap E, 2 horizontal gap F), bit 2 the E passed down extends (else
+ * it opens from H), bit 3 the F passed right extends (else it opens from H),
+ * bit 7 the cell is dead (below the X-drop bound). */
+enum { TB_DIAG = 0, TB_E = 1, TB_F = 2, TB_EEXT = 4, TB_FEXT = 8, TB_DEAD = 128 };
+
+typedef struct tb_rows {
+    int32_t *first, *end; /* per row a (0..rows): band [first, end) */
+    int64_t *at;          /* per row: offset of column `first` in dir */
+    uint8_t *dir;
+    int64_t n_dir, cap_dir;
+    int32_t rows;
+} tb_rows;
+
+static int tb_put(tb_rows *t, uint8_t v) {
+    if (t->n_dir == t->cap_dir) {
+        int64_t c = t->cap_dir ? 2 * t->cap_dir : 4096;
+        uint8_t *p = (uint8_t *)realloc(t->dir, (size_t)c);
+        if (!p) return -1;
+        t->dir = p;
+        t->cap_dir = c;
+    }
+    t->dir[t->n_dir++] = v;
+    return 0;
+}
+
+/* The banded X-drop DP of semi_gapped with every computed cell's direction
+ * kept (row 0 is the gap along the first row from the origin). */
+static int32_t tb_dp(const uint8_t *A, const uint8_t *B, int32_t M, int32_t N, int32_t reverse,
+                     int32_t gap_open, int32_t gap_extend, int32_t xdrop, int32_t *a_best, int32_t *b_best,
+                     tb_rows *t) {
+    const int32_t goe = gap_open + gap_extend;
+    if (xdrop < goe) xdrop = goe;
+    *a_best = 0;
+    *b_best = 0;
+    t->rows = 0;
+    t->n_dir = 0;
+    if (M <= 0 || N <= 0) return 0;
+    int32_t *Hb = (int32_t *)malloc(sizeof(int32_t) * (size_t)(N + 2));
+    int32_t *Eb = (int32_t *)malloc(sizeof(int32_t) * (size_t)(N + 2));
+    t->first = (int32_t *)malloc(sizeof(int32_t) * (size_t)(M + 1));
+    t->end = (int32_t *)malloc(sizeof(int32_t) * (size_t)(M + 1));
+    t->at = (int64_t *)malloc(sizeof(int64_t) * (size_t)(M + 1));
+    if (!Hb || !Eb || !t->first || !t->end || !t->at) {
+        free(Hb);
+        free(Eb);
+        return INT32_MIN;
+    }
+    int32_t score = -goe, i;
+    Hb[0] = 0;
+    Eb[0] = -goe;
+    t->first[0] = 0;
+    t->at[0] = 0;
+    tb_put(t, TB_DIAG); /* the origin */
+    for (i = 1; i <= N; i++) {
+        if (score < -xdrop) break;
+        Hb[i] = score;
+        Eb[i] = score - goe;
+        score -= gap_extend;
+        tb_put(t, (uint8_t)(TB_F | (i > 1 ? 0 : 0) | TB_FEXT)); /* along row 0 from the origin */
+    }
+    t->end[0] = i;
+    t->rows = 1;
+    int32_t b_size = i, first = 0, best = 0;
+    for (int32_t a = 1; a <= M; a++) {
+        const int32_t *row = ORC_BLOSUM62[reverse ? A[M - a] : A[a]];
+        int32_t h = ORC_NEG, f = ORC_NEG, last = first;
+        t->first[a] = first;
+        t->at[a] = t->n_dir;
+        for (int32_t b = first; b < b_size; b++) {
+            const int32_t diag = h;
+            int32_t e = Eb[b];
+            int32_t next = ORC_NEG;
+            if (b + 1 <= N) next = Hb[b] + row[reverse ? B[N - 1 - b] : B[b + 1]];
+            uint8_t d = TB_DIAG;
+            if (h < e) { h = e; d = TB_E; }
+            if (h < f) { h = f; d = TB_F; }
+            if (best - h > xdrop) {
+                if (b == first) first++;
+                else Hb[b] = ORC_NEG;
+                d = TB_DEAD;
+            } else {
+                last = b;
+                if (h > best) { best = h; *a_best = a; *b_best = b; }
+                f -= gap_extend;
+                e -= gap_extend;
+                if (!(h - goe > e)) d |= TB_EEXT;
+                if (!(h - goe > f)) d |= TB_FEXT;
+                Eb[b] = imax(h - goe, e);
+                f = imax(h - goe, f);
+                Hb[b] = h;
+            }
+            (void)diag;
+            tb_put(t, d);
+            h = next;
+        }
+        int32_t row_end = b_size;
+        if (first == b_size) {
+            t->end[a] = row_end;
+            t->rows = a + 1;
+            break;
+        }
+        if (last < b_size - 1) {
+            b_size = last + 1;
+        } else {
+            while (f >= best - xdrop && b_size <= N) {
+                Hb[b_size] = f;
+                Eb[b_size] = f - goe;
+                f -= gap_extend;
+                b_size++;
+                tb_put(t, (uint8_t)(TB_F | TB_FEXT)); /* the row gap continues */
+            }
+            row_end = b_size;
+        }
+        if (b_size <= N) {
+            Hb[b_size] = ORC_NEG;
+            Eb[b_size] = ORC_NEG;
+            b_size++;
+            tb_put(t, TB_DEAD); /* sentinel column */
+            row_end = b_size;
+        }
+        t->end[a] = row_end;
+        t->rows = a + 1;
+    }
+    free(Hb);
+    free(Eb);
+    return best;
+}
+
+typedef struct tb_walk {
+    int32_t pairs, identities, positives, gaps, gap_opens;
+    int last_move; /* move next to the origin: 0 pair, 1 vertical gap, 2 horizontal gap */
+    char *ops;     /* optional: moves from the best cell back to the origin */
+    int32_t n_ops, cap_ops;
+} tb_walk;
+
+static uint8_t tb_at(const tb_rows *t, int32_t a, int32_t b, int *ok) {
+    if (a < 0 || a >= t->rows || b < t->first[a] || b >= t->end[a]) {
+        *ok = 0;
+        return TB_DEAD;
+    }
+    return t->dir[t->at[a] + (b - t->first[a])];
+}
+
+/* Walks from (a, b) back to the origin; letters A[row], B[col] as in tb_dp. */
+static int tb_walk_back(const tb_rows *t, const uint8_t *A, const uint8_t *B, int32_t M, int32_t N, int32_t reverse,
+                        int32_t a, int32_t b, tb_walk *w) {
+    char *ops = w->ops;
+    const int32_t cap = w->cap_ops;
+    memset(w, 0, sizeof(*w));
+    w->ops = ops;
+    w->cap_ops = cap;
+    w->last_move = -1;
+    int state = 0; /* 0 H, 1 E, 2 F */
+    int prev_move = -1, ok = 1;
+    int64_t guard = (int64_t)(M + 1) * (N + 1) + 8;
+    while ((a > 0 || b > 0) && guard-- > 0) {
+        int move;
+        if (state == 0) {
+            if (a == 0) { state = 2; continue; } /* row 0: gap from the origin */
+            const uint8_t d = tb_at(t, a, b, &ok);
+            if (!ok || (d & TB_DEAD)) return -1;
+            const int src = d & 3;
+            if (src == TB_DIAG) {
+                const uint8_t x = reverse ? A[M - a] : A[a], y = reverse ? B[N - b] : B[b];
+                w->pairs++;
+                if (x == y) w->identities++;
+                if (ORC_BLOSUM62[x][y] > 0) w->positives++;
+                move = 0;
+                a--;
+                b--;
+            } else {
+                state = src == TB_E ? 1 : 2;
+                continue;
+            }
+        } else if (state == 1) { /* E at (a, b): from the cell above */
+            const uint8_t d = a - 1 == 0 ? 0 : tb_at(t, a - 1, b, &ok);
+            if (!ok) return -1;
+            move = 1;
+            w->gaps++;
+            if (a - 1 == 0 || !(d & TB_EEXT)) state = 0;
+            a--;
+        } else { /* F at (a, b): from the cell on the left */
+            const uint8_t d = tb_at(t, a, b - 1, &ok);
+            if (!ok) return -1;
+            move = 2;
+            w->gaps++;
+            if (!(d & TB_FEXT) || (a == 0 && b - 1 == 0)) state = 0;
+            b--;
+        }
+        if (move != 0 && move != prev_move) w->gap_opens++;
+        prev_move = move;
+        w->last_move = move;
+        if (w->ops && w->n_ops < w->cap_ops) w->ops[w->n_ops++] = move == 0 ? 'M' : move == 1 ? 'I' : 'D';
+    }
+    return (a == 0 && b == 0) ? 0 : -1;
+}
+
+int orc_traceback_ops(const uint8_t *query, int32_t qlen, const uint8_t *subject, int32_t slen, int32_t q_off,
+                      int32_t s_off, int32_t gap_open, int32_t gap_extend, int32_t xdrop, orc_tb *out, char *ops,
+                      int32_t ops_cap, int32_t *n_ops) {
+    memset(out, 0, sizeof(*out));
+    tb_rows t;
+    memset(&t, 0, sizeof(t));
+    int32_t al, bl, ar = 0, br = 0, right = 0;
+    tb_walk wl, wr;
+    memset(&wl, 0, sizeof(wl));
+    memset(&wr, 0, sizeof(wr));
+    wr.last_move = -1;
+    /* the left walk runs from the leftmost column: its moves are in order;
+     * the right walk's moves are reversed into the tail */
+    wl.ops = ops;
+    wl.cap_ops = ops ? ops_cap : 0;
+    char *rops = ops ? (char *)malloc((size_t)(ops_cap > 0 ? ops_cap : 1)) : NULL;
+    wr.ops = rops;
+    wr.cap_ops = rops ? ops_cap : 0;
+    int32_t left = tb_dp(query, subject, q_off + 1, s_off + 1, 1, gap_open, gap_extend, xdrop, &al, &bl, &t);
+    int rc = left == INT32_MIN ? -1 : tb_walk_back(&t, query, subject, q_off + 1, s_off + 1, 1, al, bl, &wl);
+    if (rc == 0 && q_off < qlen - 1 && s_off < slen - 1) {
+        free(t.first); free(t.end); free(t.at);
+        t.first = NULL; t.end = NULL; t.at = NULL;
+        right = tb_dp(query + q_off, subject + s_off, qlen - q_off - 1, slen - s_off - 1, 0, gap_open, gap_extend,
+                      xdrop, &ar, &br, &t);
+        rc = right == INT32_MIN ? -1 : tb_walk_back(&t, query + q_off, subject + s_off, qlen - q_off - 1,
+                                                    slen - s_off - 1, 0, ar, br, &wr);
+    }
+    free(t.first); free(t.end); free(t.at); free(t.dir);
+    if (ops && n_ops) {
+        int32_t n = wl.n_ops;
+        for (int32_t k = wr.n_ops - 1; k >= 0 && n < ops_cap; k--) ops[n++] = rops[k];
+        *n_ops = n;
+    }
+    free(rops);
+    if (rc != 0) return -1;
+    out->score = left + right;
+    out->q_start = q_off + 1 - al;
+    out->q_end = q_off + ar + 1;
+    out->s_start = s_off + 1 - bl;
+    out->s_end = s_off + br + 1;
+    out->identities = wl.identities + wr.identities;
+    out->positives = wl.positives + wr.positives;
+    out->gaps = wl.gaps + wr.gaps;
+    out->length = wl.pairs + wr.pairs + out->gaps;
+    out->mismatches = wl.pairs + wr.pairs - out->identities;
+    out->gap_opens = wl.gap_opens + wr.gap_opens;
+    /* one gap run across the start point is one opening */
+    if (wl.last_move > 0 && wl.last_move == wr.last_move) out->gap_opens--;
+    return 0;
+}
+
+int orc_traceback(const uint8_t *query, int32_t qlen, const uint8_t *subject, int32_t slen, int32_t q_off,
+                  int32_t s_off, int32_t gap_open, int32_t gap_extend, int32_t xdrop, orc_tb *out) {
+    return orc_traceback_ops(query, qlen, subject, slen, q_off, s_off, gap_open, gap_extend, xdrop, out, NULL, 0,
+                             NULL);
+}
+
 /* --------------------------------------------------- purge and final sort */
 
 static int cmp_start(const void *x, const void *y) {

@@ -111,6 +111,27 @@ void orc_result_copy_hsps(const orc_result *r, orc_hsp *out);
 void orc_result_copy_inits(const orc_result *r, orc_init *out);
 void orc_result_free(orc_result *r);
 
+/* Traceback of one gapped HSP (the published gapped-BLAST traceback:
+ * X-drop alignment left and right of the start point with the path kept).
+ * The DP is the banded X-drop DP above with the final X-drop; each live cell
+ * records where its score came from (diagonal beats a vertical gap beats a
+ * horizontal gap on ties; a gap state extends rather than opens on ties);
+ * the path runs back from the first best cell to the origin. */
+typedef struct orc_tb {
+    int32_t score;
+    int32_t q_start, q_end, s_start, s_end;  /* 0-based, ends exclusive */
+    int32_t length;                          /* aligned columns */
+    int32_t identities, positives, mismatches;
+    int32_t gap_opens, gaps;
+} orc_tb;
+int orc_traceback(const uint8_t *query, int32_t qlen, const uint8_t *subject, int32_t slen, int32_t q_off,
+                  int32_t s_off, int32_t gap_open, int32_t gap_extend, int32_t xdrop, orc_tb *out);
+/* The same, also writing the alignment's moves in query order ('M' pair,
+ * 'I' query residue against a gap, 'D' subject residue against a gap). */
+int orc_traceback_ops(const uint8_t *query, int32_t qlen, const uint8_t *subject, int32_t slen, int32_t q_off,
+                      int32_t s_off, int32_t gap_open, int32_t gap_extend, int32_t xdrop, orc_tb *out, char *ops,
+                      int32_t ops_cap, int32_t *n_ops);
+
 /* Karlin-Altschul arithmetic (restated published formulas). */
 double orc_evalue(int32_t score, double lambda, double K, double searchsp);
 int32_t orc_length_adjustment(double K, double logK, double alpha_d_lambda, double beta,
