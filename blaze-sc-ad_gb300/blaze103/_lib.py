@@ -74,6 +74,8 @@ class BlazeStats(ctypes.Structure):
         ("device_ms", ctypes.c_float), ("kernel_launches", ctypes.c_uint32),
         ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
         ("graph_replays", ctypes.c_uint32), ("graph_builds", ctypes.c_uint32),
+        ("traceback_ms", ctypes.c_float), ("traceback_hsps", ctypes.c_uint32),
+        ("traceback_cells", ctypes.c_uint64),
     ]
 
     def as_dict(self) -> dict:

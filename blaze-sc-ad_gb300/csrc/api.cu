@@ -1213,6 +1213,9 @@ extern "C" int blaze_search_traceback(blaze_search *s, const blaze_query *q, con
         items[i] = TbItem{sub, h.q_gapped_start, h.s_gapped_start, 0u};
     }
     std::vector<TbOut> outs(n);
+    s->stats.traceback_ms = 0.f;
+    s->stats.traceback_hsps = static_cast<uint32_t>(n);
+    s->stats.traceback_cells = 0;
     if (n > 0) {
         const int blocks = s->n_sm;
         const size_t warps = static_cast<size_t>(blocks) * kTracebackWarpsPerBlock;
@@ -1247,14 +1250,20 @@ extern "C" int blaze_search_traceback(blaze_search *s, const blaze_query *q, con
             ta.row_cap = row_cap;
             ta.cursor = s->tb_cursor.p;
             BLAZE_CUDA_TRY(cudaMemsetAsync(s->tb_cursor.p, 0, sizeof(unsigned long long), s->stream));
+            BLAZE_CUDA_TRY(cudaEventRecord(s->ev[1], s->stream));
             BLAZE_CUDA_TRY(launch_traceback(ta, blocks, s->stream));
+            BLAZE_CUDA_TRY(cudaEventRecord(s->ev[2], s->stream));
             s->stats.kernel_launches += 1;
             BLAZE_CUDA_TRY(cudaMemcpyAsync(outs.data(), s->tb_out.p, sizeof(TbOut) * n, cudaMemcpyDeviceToHost,
                                            s->stream));
             BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
             s->stats.d2h_bytes += sizeof(TbOut) * n;
+            float ms = 0.f;
+            BLAZE_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev[1], s->ev[2]));
+            s->stats.traceback_ms += ms;
             bool overflow = false;
             for (const TbOut &o : outs) {
+                s->stats.traceback_cells += static_cast<uint64_t>(o.cells);
                 if (o.status == 2) return BLAZE_ERR_INTERNAL;
                 overflow |= o.status == 1;
             }

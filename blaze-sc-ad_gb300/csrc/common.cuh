@@ -156,6 +156,7 @@ struct TbOut {
     int32_t score, q_start, q_end, s_start, s_end;
     int32_t length, identities, positives, mismatches, gap_opens, gaps;
     int32_t status;  // 0 done, 1 direction buffer too small, 2 inconsistent path
+    int32_t cells;   // DP cells computed (left and right)
 };
 
 struct TracebackArgs {

@@ -44,7 +44,7 @@ template <bool REV>
 __device__ int32_t xdrop_dp_dirs(const uint8_t *__restrict__ A, const uint8_t *__restrict__ B, int32_t M,
                                  int32_t N, int32_t gap_open, int32_t gap_extend, int32_t xdrop, const int32_t *mat,
                                  int32_t *Hb, int32_t *Eb, int32_t *a_best, int32_t *b_best, DirRows &d,
-                                 int32_t *rows_used) {
+                                 int32_t *rows_used, int32_t *cells) {
     const int lane = threadIdx.x & 31;
     const int32_t goe = gap_open + gap_extend, ge = gap_extend;
     if (xdrop < goe) xdrop = goe;
@@ -78,6 +78,7 @@ __device__ int32_t xdrop_dp_dirs(const uint8_t *__restrict__ A, const uint8_t *_
         }
         const int32_t *row = mat + kAlphabet * (REV ? A[M - a] : A[a]);
         const int32_t row_first = first;
+        *cells += bsize - first;
         int32_t carry_p = kNeg, carry_best = best, carry_hold = kNeg;
         int32_t first_alive = -1, last_alive = -1, row_best = best, row_best_b = -1;
         for (int32_t c0 = first; c0 < bsize; c0 += 32) {
@@ -296,16 +297,16 @@ __global__ void __launch_bounds__(kTracebackWarpsPerBlock * 32) traceback_kernel
         const int32_t slen = static_cast<int32_t>(a.off[it.subject + 1] - o0);
         const int32_t q_off = it.q_off, s_off = it.s_off;
         d.overflow = false;
-        int32_t al, bl, ar = 0, br = 0, right = 0, rows;
+        int32_t al, bl, ar = 0, br = 0, right = 0, rows, cells = 0;
         TbOut o{};
         const int32_t left = xdrop_dp_dirs<true>(a.q, sub, q_off + 1, s_off + 1, a.gap_open, a.gap_extend, a.xdrop,
-                                                 mat, Hb, Eb, &al, &bl, d, &rows);
+                                                 mat, Hb, Eb, &al, &bl, d, &rows, &cells);
         Walk wl{0, 0, 0, 0, 0, -1, true}, wr{0, 0, 0, 0, 0, -1, true};
         if (!d.overflow && lane == 0) wl = walk_back<true>(d, rows, a.q, sub, q_off + 1, s_off + 1, al, bl, mat);
         __syncwarp();
         if (!d.overflow && q_off < a.qlen - 1 && s_off < slen - 1) {
             right = xdrop_dp_dirs<false>(a.q + q_off, sub + s_off, a.qlen - q_off - 1, slen - s_off - 1, a.gap_open,
-                                         a.gap_extend, a.xdrop, mat, Hb, Eb, &ar, &br, d, &rows);
+                                         a.gap_extend, a.xdrop, mat, Hb, Eb, &ar, &br, d, &rows, &cells);
             if (!d.overflow && lane == 0)
                 wr = walk_back<false>(d, rows, a.q + q_off, sub + s_off, a.qlen - q_off - 1, slen - s_off - 1, ar,
                                       br, mat);
@@ -323,6 +324,7 @@ __global__ void __launch_bounds__(kTracebackWarpsPerBlock * 32) traceback_kernel
             o.mismatches = wl.pairs + wr.pairs - o.identities;
             o.gap_opens = wl.gap_opens + wr.gap_opens - ((wl.last_move > 0 && wl.last_move == wr.last_move) ? 1 : 0);
             o.status = d.overflow ? 1 : ((wl.ok && wr.ok) ? 0 : 2);
+            o.cells = cells;
             a.out[t] = o;
         }
         __syncwarp();

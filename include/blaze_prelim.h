@@ -112,6 +112,9 @@ typedef struct blaze_stats {
     uint64_t d2h_bytes; /* device->host bytes of the run */
     uint32_t graph_replays; /* passes launched from an already built CUDA graph */
     uint32_t graph_builds;  /* passes that captured (or updated) the CUDA graph */
+    float traceback_ms;     /* last blaze_search_traceback: its kernel launches (CUDA events) */
+    uint32_t traceback_hsps;
+    uint64_t traceback_cells; /* DP cells of the traceback (left and right, all passes) */
 } blaze_stats;
 
 const char *blaze_status_string(int status);

@@ -93,3 +93,23 @@ def test_traceback_buffer_regrowth(monkeypatch):
     q = synth.random_residues(rng, 700)
     res, off = _db_with_homologs(15, q, n=300)
     _check(q, res, off)
+
+
+def test_traceback_to_tabular():
+    from blaze103 import tabular
+
+    w = synth.make_workload(0, scale=0.1)
+    db = blaze103.SeqSrc(w.residues, w.offsets)
+    ps = blaze103.PrelimSearch(db)
+    q = w.queries[0]
+    p = blaze103.default_params(len(q), db)
+    ps.run(q, p)
+    tb = ps.traceback(q, p)
+    text = tabular.format_tabular(tb, "query1", lambda oid: f"subject{oid}", outfmt=7)
+    lines = [ln for ln in text.splitlines() if not ln.startswith("#")]
+    assert len(lines) == len(tb) > 0
+    cols = lines[0].split("\t")
+    assert len(cols) == 12 and float(cols[2]) > 30.0
+    assert ps.stats()["traceback_ms"] > 0
+    ps.close()
+    db.close()
