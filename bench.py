@@ -180,7 +180,7 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    w = synth.make_workload(1, scale=args.scale)
+    w = synth.make_workload("plain-db-scale", scale=args.scale)
     rates = []
     for _ in range(args.warmup):
         cpu_sample_run(w, w.queries, args.ref_frac, threads, w.total_residues, w.n_subjects)
@@ -201,7 +201,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic (seeded; config 1 shape)",
+        "data": "synthetic (seeded; plain-db-scale workload: 8 queries, 2M subjects)",
         "config": {"workload": "plain drop-in, 8 queries (100-1000 aa) vs 2M subjects / 0.7G residues",
                    "db_subjects": w.n_subjects, "db_residues": w.total_residues,
                    "queries": [len(q) for q in w.queries], "parallelism": "host threads",
@@ -217,13 +217,13 @@ def run_reference(args, rank, world):
 
 def run_batched(args, rank, world, local):
     """Batched form vs the plain path on the same queries and database
-    (config-2 shape: query lengths log-normal, median 350, clipped 50-2,000;
+    (batched workload: query lengths log-normal, median 350, clipped 50-2,000;
     10% planted homologs), both timed with CUDA events."""
     import blaze103
     from blaze103 import synth
 
     scale = args.scale if args.scale != 1.0 else 0.02
-    w = synth.make_workload(2, scale=scale, n_queries=args.queries, seed=2 + 7919 * rank)
+    w = synth.make_workload("batched", scale=scale, n_queries=args.queries, seed=2 + 7919 * rank)
     db_total, db_n = w.total_residues * world, w.n_subjects * world
     db = blaze103.SeqSrc(w.residues, w.offsets, device=local)
     ps = blaze103.PrelimSearch(db)
@@ -261,11 +261,11 @@ def run_batched(args, rank, world, local):
         "value": nq * R / b_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": b_s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic (seeded; config-2 shape scaled)",
+        "data": "synthetic (seeded; batched workload: 512 queries, database scaled)",
         "config": {"workload": f"batched: {nq} queries (log-normal median 350, 50-2000 aa) vs "
                                f"{w.n_subjects} subjects / {R} residues, one launch per stage",
                    "db_subjects": w.n_subjects, "db_residues": R, "queries": nq,
-                   "scale_of_config2": scale},
+                   "database_scale": scale},
         "plain_same_workload": {"value": nq * R / p_s, "ms_per_step": p_s * 1e3},
         "stages_ms_per_step": {"scan": last["scan_ms"], "gapped": last["gapped_ms"]},
         "work_per_step": {k: last[k] for k in ("word_hits", "ungapped_extensions", "init_hsps",
@@ -284,7 +284,8 @@ def run_batched(args, rank, world, local):
 
 
 def run_serve(args, rank, world, local):
-    """Serving loop under Poisson arrivals (config-4 shape, database scaled):
+    """Serving loop under Poisson arrivals (serving workload: query lengths
+    log-normal, median 350, 30-5,000; database scaled):
     for each offered rate, queries arrive at exponential gaps, are batched on
     the fly by the library's serving loop and completed; reports throughput
     and p50/p99 latency (submission to completion), beside the same arrivals
@@ -293,7 +294,7 @@ def run_serve(args, rank, world, local):
     from blaze103 import synth
 
     scale = args.scale if args.scale != 1.0 else 0.01
-    w = synth.make_workload(4, scale=scale, seed=4 + 7919 * rank)
+    w = synth.make_workload("serving", scale=scale, seed=4 + 7919 * rank)
     rng = np.random.default_rng(44 + rank)
     pool = [synth.random_residues(rng, int(L))
             for L in synth.lognormal_lengths(rng, 512, 350, 0.82, 30, 5000)]
@@ -339,10 +340,10 @@ def run_serve(args, rank, world, local):
         "metric": "DB residues/s per query, served under Poisson arrivals (aggregate); p50/p99 latency",
         "value": top["residues_per_s"], "unit": UNIT, "n_gpus": world, "steps": len(rates),
         "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded; config-4 shape scaled)",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded; serving workload, database scaled)",
         "config": {"workload": f"serving: Poisson arrivals at {args.rates} q/s, query lengths log-normal "
                                f"(median 350, 30-5000) vs {w.n_subjects} subjects / {R} residues",
-                   "db_subjects": w.n_subjects, "db_residues": R, "scale_of_config4": scale,
+                   "db_subjects": w.n_subjects, "db_residues": R, "database_scale": scale,
                    "server": batched_cfg},
         "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
         "sweep": sweep,
@@ -359,13 +360,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="blaze", choices=["blaze", "reference"])
-    ap.add_argument("--scale", type=float, default=1.0, help="database size relative to config 1")
+    ap.add_argument("--scale", type=float, default=1.0, help="database size relative to the default workload (2M subjects)")
     ap.add_argument("--cpu-frac", type=float, default=0.25, help="cpu_baseline sample fraction")
     ap.add_argument("--ref-frac", type=float, default=0.02, help="reference arm sample fraction per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="plain", choices=["plain", "batched", "serve"],
                     help="plain: the drop-in, one query per launch sequence (the headline line); "
-                         "batched: many queries per launch against the config-2 shaped database")
+                         "batched: many queries per launch against a 5M-subject-shaped database, scaled")
     ap.add_argument("--queries", type=int, default=512, help="batched mode: queries per batch")
     ap.add_argument("--rates", default="10,100,500,2000", help="serve mode: arrival rates, queries/s")
     ap.add_argument("--duration", type=float, default=2.0, help="serve mode: seconds of arrivals per rate")
@@ -390,7 +391,7 @@ def main():
     from blaze103 import synth
 
     group = Group(world, local)
-    w = synth.make_workload(1, scale=args.scale, seed=1 + 7919 * rank)
+    w = synth.make_workload("plain-db-scale", scale=args.scale, seed=1 + 7919 * rank)
     db_total, db_n = w.total_residues * world, w.n_subjects * world  # E-values over the global DB
     db = blaze103.SeqSrc(w.residues, w.offsets, device=local)
     ps = blaze103.PrelimSearch(db)

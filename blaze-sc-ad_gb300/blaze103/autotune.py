@@ -26,12 +26,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 TUNING_PATH = os.path.join(HERE, "tuning.json")
 
-# shapes: (kind, workload config, scale of its database, queries)
+# shapes: (kind, synthetic workload, scale of its database, queries)
 SHAPES = {
-    "plain-config1": ("plain", 1, 0.1, 8),
-    "batched-config2": ("batched", 2, 0.02, 512),
-    "batched-config2-small": ("batched", 2, 0.02, 64),
-    "serving-config4": ("batched", 4, 0.01, 32),
+    "plain-db-scale": ("plain", "plain-db-scale", 0.1, 8),
+    "batched-512": ("batched", "batched", 0.02, 512),
+    "batched-64": ("batched", "batched", 0.02, 64),
+    "serving-32": ("batched", "serving", 0.01, 32),
 }
 
 GRID = {
@@ -83,11 +83,12 @@ def tune_shape(name: str, reps: int = 3, quick: bool = False) -> dict:
     import blaze103
     from blaze103 import synth
 
-    kind, config, scale, nq = SHAPES[name]
-    w = synth.make_workload(config, scale=scale, n_queries=nq, seed=config)
-    rng = np.random.default_rng(config)
+    kind, workload, scale, nq = SHAPES[name]
+    seed = synth.WORKLOADS[workload]["index"]
+    w = synth.make_workload(workload, scale=scale, n_queries=nq, seed=seed)
+    rng = np.random.default_rng(seed)
     queries = list(w.queries)
-    while len(queries) < nq:  # configs with fewer queries than the batch: draw more
+    while len(queries) < nq:  # workloads with fewer queries than the batch: draw more
         queries.append(synth.random_residues(rng, int(synth.lognormal_lengths(rng, 1, 350, 0.82, 30, 5000)[0])))
     queries = queries[:nq]
     db = blaze103.SeqSrc(w.residues, w.offsets)

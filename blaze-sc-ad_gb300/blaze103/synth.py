@@ -112,19 +112,22 @@ class Workload:
         return int(self.offsets[-1])
 
 
-CONFIGS = {
-    0: dict(name="plain-small", query_lengths=[300], n_subjects=20_000, clip=(30, 5000),
-            homolog_frac=0.01, identity=(0.40, 0.40), lowcomplex_frac=0.0),
-    1: dict(name="plain-db-scale", query_lengths=[100, 200, 300, 500, 700, 800, 900, 1000],
-            n_subjects=2_000_000, clip=(30, 5000), homolog_frac=0.01, identity=(0.40, 0.40),
-            lowcomplex_frac=0.0),
-    2: dict(name="batched", query_lengths=("lognormal", 512, 350, 50, 2000), n_subjects=5_000_000,
-            clip=(30, 5000), homolog_frac=0.10, identity=(0.40, 0.40), lowcomplex_frac=0.0),
-    3: dict(name="overflow-stress", query_lengths=("uniform", 64, 2000, 5000), n_subjects=500_000,
-            clip=(30, 35000), homolog_frac=0.25, identity=(0.30, 0.60), lowcomplex_frac=0.20),
-    4: dict(name="serving", query_lengths=("lognormal", 256, 350, 30, 5000), n_subjects=10_000_000,
-            clip=(30, 5000), homolog_frac=0.01, identity=(0.40, 0.40), lowcomplex_frac=0.0),
+# The workloads the benchmark and tests draw (sizes at scale 1.0). Each has a
+# fixed index, which is also its default random seed.
+WORKLOADS = {
+    "plain-small": dict(index=0, query_lengths=[300], n_subjects=20_000, clip=(30, 5000),
+                        homolog_frac=0.01, identity=(0.40, 0.40), lowcomplex_frac=0.0),
+    "plain-db-scale": dict(index=1, query_lengths=[100, 200, 300, 500, 700, 800, 900, 1000],
+                           n_subjects=2_000_000, clip=(30, 5000), homolog_frac=0.01, identity=(0.40, 0.40),
+                           lowcomplex_frac=0.0),
+    "batched": dict(index=2, query_lengths=("lognormal", 512, 350, 50, 2000), n_subjects=5_000_000,
+                    clip=(30, 5000), homolog_frac=0.10, identity=(0.40, 0.40), lowcomplex_frac=0.0),
+    "overflow-stress": dict(index=3, query_lengths=("uniform", 64, 2000, 5000), n_subjects=500_000,
+                            clip=(30, 35000), homolog_frac=0.25, identity=(0.30, 0.60), lowcomplex_frac=0.20),
+    "serving": dict(index=4, query_lengths=("lognormal", 256, 350, 30, 5000), n_subjects=10_000_000,
+                    clip=(30, 5000), homolog_frac=0.01, identity=(0.40, 0.40), lowcomplex_frac=0.0),
 }
+_BY_INDEX = {w["index"]: name for name, w in WORKLOADS.items()}
 
 
 def _query_lengths(rng, spec) -> list:
@@ -137,12 +140,13 @@ def _query_lengths(rng, spec) -> list:
     return [int(x) for x in spec]
 
 
-def make_workload(config: int, scale: float = 1.0, seed: int | None = None,
+def make_workload(workload, scale: float = 1.0, seed: int | None = None,
                   n_queries: int | None = None, median: float = 250.0,
                   sigma: float = 0.82) -> Workload:
-    """Build config `config` (0-4) with n_subjects scaled by `scale`."""
-    c = dict(CONFIGS[config])
-    rng = np.random.default_rng(config if seed is None else seed)
+    """Build a workload (its name, or its index) with n_subjects scaled by `scale`."""
+    name = _BY_INDEX[workload] if isinstance(workload, int) else workload
+    c = dict(WORKLOADS[name])
+    rng = np.random.default_rng(c["index"] if seed is None else seed)
     qlens = _query_lengths(rng, c["query_lengths"])
     if n_queries is not None:
         qlens = qlens[:n_queries]
@@ -174,6 +178,6 @@ def make_workload(config: int, scale: float = 1.0, seed: int | None = None,
         hom = hom[:L]
         pos = int(offsets[i]) + int(rng.integers(0, L - len(hom) + 1))
         residues[pos:pos + len(hom)] = hom
-    return Workload(name=c["name"], queries=queries, residues=residues, offsets=offsets,
-                    planted=planted, meta=dict(config=config, scale=scale, n_subjects=n,
+    return Workload(name=name, queries=queries, residues=residues, offsets=offsets,
+                    planted=planted, meta=dict(workload=name, scale=scale, n_subjects=n,
                                               total_residues=int(offsets[-1])))

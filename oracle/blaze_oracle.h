@@ -20,7 +20,8 @@
  *   - score-only semi-gapped X-drop DP ....... BLAZE_gpu/gpuBLAZE.cu:356-677 (X-drop form)
  *   - per-subject pipeline order (word finder, gapped score, purge, sort,
  *     E-values, prelim reap) ................. BLAZE_ncbi/blast_engine.c:654-853, 896-932, 1423-1477
- * Every choice that the reference leaves to NCBI code is listed in the design doc.
+ * Where the reference leaves a choice to NCBI code, the function restating
+ * it says which published rule it follows.
  */
 #ifndef BLAZE_ORACLE_H
 #define BLAZE_ORACLE_H

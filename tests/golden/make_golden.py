@@ -25,7 +25,7 @@ PARAM_KEYS = ["word_threshold", "window", "ungapped_xdrop", "ungapped_cutoff", "
 
 
 def cases():
-    w = synth.make_workload(0, scale=0.02)
+    w = synth.make_workload("plain-small", scale=0.02)
     yield "config0_scale002", w.queries[0], w.residues, w.offsets, (7_000_000, 20_000)
     rng = np.random.default_rng(77)
     alpha = np.array([1, 11, 17], dtype=np.uint8)

@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 
 def test_config0_scaled():
-    w = synth.make_workload(0, scale=0.25)
+    w = synth.make_workload("plain-small", scale=0.25)
     got, ref, stats = compare(w.queries[0], w.residues, w.offsets)
     assert len(got) > 0 and stats["dp_cells"] > 0
     assert np.isin(w.planted, got["oid"]).mean() > 0.9
@@ -55,7 +55,7 @@ def test_tiny_queries():
 
 
 def test_unsorted_database_keeps_oids():
-    w = synth.make_workload(0, scale=0.05)
+    w = synth.make_workload("plain-small", scale=0.05)
     n = w.n_subjects
     perm = np.random.default_rng(9).permutation(n)
     seqs = [w.residues[int(w.offsets[i]):int(w.offsets[i + 1])] for i in perm]
@@ -86,19 +86,19 @@ def test_capacity_regrowth(monkeypatch):
     monkeypatch.setenv("BLAZE_INITIAL_SCRATCH_CAP", "2")
     monkeypatch.setenv("BLAZE_INITIAL_INIT_CAP", "3")
     monkeypatch.setenv("BLAZE_INITIAL_OUT_CAP", "3")
-    w = synth.make_workload(0, scale=0.05)
+    w = synth.make_workload("plain-small", scale=0.05)
     got, _, stats = compare(w.queries[0], w.residues, w.offsets)
     assert stats["reruns"] >= 1 and len(got) > 3
 
 
 def test_long_subjects_and_queries():
-    w = synth.make_workload(3, scale=0.001, n_queries=2)
+    w = synth.make_workload("overflow-stress", scale=0.001, n_queries=2)
     for q in w.queries:
         compare(q, w.residues, w.offsets)
 
 
 def test_one_call_host_buffers_and_small_output():
-    w = synth.make_workload(0, scale=0.05)
+    w = synth.make_workload("plain-small", scale=0.05)
     q = w.queries[0]
     db = blaze103.SeqSrc(w.residues, w.offsets)
     ps = blaze103.PrelimSearch(db)
@@ -117,7 +117,7 @@ def test_one_call_host_buffers_and_small_output():
 
 
 def test_invalid_inputs_rejected():
-    w = synth.make_workload(0, scale=0.01)
+    w = synth.make_workload("plain-small", scale=0.01)
     db = blaze103.SeqSrc(w.residues, w.offsets)
     bad = np.array([1, 2, 0, 4], dtype=np.uint8)
     with pytest.raises(ValueError):

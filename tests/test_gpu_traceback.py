@@ -98,7 +98,7 @@ def test_traceback_buffer_regrowth(monkeypatch):
 def test_traceback_to_tabular():
     from blaze103 import tabular
 
-    w = synth.make_workload(0, scale=0.1)
+    w = synth.make_workload("plain-small", scale=0.1)
     db = blaze103.SeqSrc(w.residues, w.offsets)
     ps = blaze103.PrelimSearch(db)
     q = w.queries[0]

@@ -171,7 +171,7 @@ def test_short_and_empty_subjects(oracle_mod):
 
 
 def test_multithreaded_equals_single_thread(oracle_mod):
-    w = synth.make_workload(0, scale=0.05)
+    w = synth.make_workload("plain-small", scale=0.05)
     p = _params(len(w.queries[0]), w.total_residues, w.n_subjects)
     a = oracle_mod.search_db(w.queries[0], w.residues, w.offsets, p, threads=1, want_inits=True)
     b = oracle_mod.search_db(w.queries[0], w.residues, w.offsets, p, threads=7, want_inits=True)
@@ -179,7 +179,7 @@ def test_multithreaded_equals_single_thread(oracle_mod):
 
 
 def test_planted_homologs_are_found(oracle_mod):
-    w = synth.make_workload(0, scale=0.1)
+    w = synth.make_workload("plain-small", scale=0.1)
     p = _params(len(w.queries[0]), w.total_residues, w.n_subjects)
     h, _ = oracle_mod.search_db(w.queries[0], w.residues, w.offsets, p, threads=4)
     found = np.isin(w.planted, h["subject"]).mean()

@@ -67,7 +67,7 @@ def test_volume_rejects_malformed(tmp_path):
 
 @pytest.mark.gpu
 def test_opened_volume_searches_like_arrays(tmp_path):
-    w = synth.make_workload(0, scale=0.05)
+    w = synth.make_workload("plain-small", scale=0.05)
     path = os.path.join(tmp_path, "cfg0")
     volume.write_volume(path, w.residues, w.offsets, version=5)
     a = blaze103.SeqSrc(w.residues, w.offsets)
