@@ -3,7 +3,9 @@
     python tests/golden/make_golden.py
 
 Each fixture holds a seeded synthetic case (query, residues, offsets), the
-search parameters, and the oracle's init hits and final HSPs for it. The
+search parameters, the oracle's init hits and final HSPs for it, and the
+oracle's traceback of those HSPs (final X-drop 64, before the E-value reap).
+The
 reference ships no golden vectors for this path, so these pin the oracle
 against its own past output (regressions), while tests/test_oracle.py pins it
 against brute force and known answers.
@@ -26,7 +28,7 @@ PARAM_KEYS = ["word_threshold", "window", "ungapped_xdrop", "ungapped_cutoff", "
 
 def cases():
     w = synth.make_workload("plain-small", scale=0.02)
-    yield "config0_scale002", w.queries[0], w.residues, w.offsets, (7_000_000, 20_000)
+    yield "plain_small_scale002", w.queries[0], w.residues, w.offsets, (7_000_000, 20_000)
     rng = np.random.default_rng(77)
     alpha = np.array([1, 11, 17], dtype=np.uint8)
     q = np.concatenate([alpha[rng.integers(0, 3, 120)], synth.random_residues(rng, 180)])
@@ -47,11 +49,28 @@ def main():
     for name, q, res, off, (dblen, dbn) in cases():
         p = oracle.default_params(len(q), dblen, dbn)
         hsps, inits = oracle.search_db(q, res, off, p, threads=4, want_inits=True)
+        traced = traced_records(q, res, off, hsps, p)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), query=np.asarray(q, np.uint8),
                             residues=np.asarray(res, np.uint8), offsets=off,
                             params=np.array([p[k] for k in PARAM_KEYS], np.int32),
-                            db_len=np.int64(dblen), db_n=np.int64(dbn), hsps=hsps, inits=inits)
-        print(name, len(res), "residues", len(inits), "init hits", len(hsps), "HSPs")
+                            db_len=np.int64(dblen), db_n=np.int64(dbn), hsps=hsps, inits=inits, traced=traced)
+        print(name, len(res), "residues", len(inits), "init hits", len(hsps), "HSPs", len(traced), "traced")
+
+
+TRACED_DTYPE = np.dtype([("subject", "<u4")] + [(f, "<i4") for f in (
+    "score", "q_start", "q_end", "s_start", "s_end", "length", "identities", "positives", "mismatches",
+    "gap_opens", "gaps")])
+
+
+def traced_records(q, res, off, hsps, p):
+    """The oracle's traceback stage over the preliminary HSPs, no E-value reap."""
+    fin = oracle.finish(hsps, dict(p, prelim_evalue=1e300))
+    rows = oracle.traceback_hsps(q, res, off, fin, p, evalue=1e300)
+    out = np.zeros(len(rows), dtype=TRACED_DTYPE)
+    for i, r in enumerate(rows):
+        for f in TRACED_DTYPE.names:
+            out[i][f] = r[f]
+    return out
 
 
 if __name__ == "__main__":

@@ -55,3 +55,43 @@ def test_gpu_matches_fixture(path):
     q.close()
     ps.close()
     db.close()
+
+
+TRACED_FIELDS = ["score", "q_start", "q_end", "s_start", "s_end", "length", "identities", "positives",
+                 "mismatches", "gap_opens", "gaps"]
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p) for p in FIXTURES])
+def test_oracle_traceback_matches_fixture(oracle_mod, path):
+    z, p = load(path)
+    pd = oracle_mod.default_params(len(z["query"]), int(z["db_len"]), int(z["db_n"]))
+    pd.update(p)
+    fin = oracle_mod.finish(z["hsps"], dict(pd, prelim_evalue=1e300))
+    rows = oracle_mod.traceback_hsps(z["query"], z["residues"], z["offsets"], fin, pd, evalue=1e300)
+    want = z["traced"]
+    assert len(rows) == len(want) > 0
+    assert [r["subject"] for r in rows] == want["subject"].tolist()
+    for f in TRACED_FIELDS:
+        assert [r[f] for r in rows] == want[f].tolist(), f
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p) for p in FIXTURES])
+def test_gpu_traceback_matches_fixture(path):
+    import blaze103
+
+    z, p = load(path)
+    db = blaze103.SeqSrc(z["residues"], z["offsets"])
+    ps = blaze103.PrelimSearch(db)
+    prm = blaze103.default_params(len(z["query"]), db_residues=int(z["db_len"]), db_subjects=int(z["db_n"]))
+    for k, v in p.items():
+        setattr(prm, k, v)
+    prm.prelim_evalue = 1e300
+    ps.run(z["query"], prm)
+    got = ps.traceback(z["query"], prm, evalue=1e300)
+    want = z["traced"]
+    assert got["oid"].tolist() == want["subject"].tolist()
+    for f in TRACED_FIELDS:
+        assert got[f].tolist() == want[f].tolist(), f
+    ps.close()
+    db.close()
