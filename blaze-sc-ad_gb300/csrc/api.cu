@@ -122,7 +122,7 @@ struct blaze_search {
     DevBuf<uint8_t> tb_dirs;
     DevBuf<int32_t> tb_rows, tb_dp;
     DevBuf<unsigned long long> tb_cursor;
-    unsigned long long tb_dir_cap = 1ull << 18;  // direction bytes per warp; doubles on overflow
+    unsigned long long tb_dir_cap = 1ull << 16;  // direction bytes per warp in a first pass
     std::vector<blaze_aligned_hsp> tb_results;
 };
 
@@ -1216,61 +1216,74 @@ extern "C" int blaze_search_traceback(blaze_search *s, const blaze_query *q, con
     s->stats.traceback_ms = 0.f;
     s->stats.traceback_hsps = static_cast<uint32_t>(n);
     s->stats.traceback_cells = 0;
-    if (n > 0) {
-        const int blocks = s->n_sm;
+    // Passes over the HSPs still to trace: the first over all of them with
+    // many warps and small direction buffers, the next ones over those whose
+    // alignment did not fit, with fewer warps and buffers four times larger.
+    std::vector<uint32_t> todo(n);
+    for (size_t i = 0; i < n; ++i) todo[i] = static_cast<uint32_t>(i);
+    unsigned long long cap = s->tb_dir_cap;
+    const uint32_t row_cap = static_cast<uint32_t>(q->qlen) + 2u;
+    const uint32_t dp_stride = std::max<uint32_t>(db->max_len, 1u) + 2u;
+    std::vector<TbItem> pass_items;
+    std::vector<TbOut> pass_out;
+    for (int attempt = 0; !todo.empty(); ++attempt) {
+        if (attempt > 12) return BLAZE_ERR_LIMIT;
+        const size_t m = todo.size();
+        const int blocks = static_cast<int>(std::min<size_t>(static_cast<size_t>(s->n_sm) * 4,
+                                                             (m + kTracebackWarpsPerBlock - 1) / kTracebackWarpsPerBlock));
         const size_t warps = static_cast<size_t>(blocks) * kTracebackWarpsPerBlock;
-        const uint32_t row_cap = static_cast<uint32_t>(q->qlen) + 2u;
-        const uint32_t dp_stride = std::max<uint32_t>(db->max_len, 1u) + 2u;
-        if ((rc = s->tb_items.ensure(n)) != BLAZE_OK) return rc;
-        if ((rc = s->tb_out.ensure(n)) != BLAZE_OK) return rc;
+        pass_items.resize(m);
+        for (size_t k = 0; k < m; ++k) pass_items[k] = items[todo[k]];
+        pass_out.resize(m);
+        if ((rc = s->tb_items.ensure(m)) != BLAZE_OK) return rc;
+        if ((rc = s->tb_out.ensure(m)) != BLAZE_OK) return rc;
         if ((rc = s->tb_rows.ensure(warps * 3 * row_cap)) != BLAZE_OK) return rc;
         if ((rc = s->tb_dp.ensure(warps * 2 * dp_stride)) != BLAZE_OK) return rc;
         if ((rc = s->tb_cursor.ensure(1)) != BLAZE_OK) return rc;
-        BLAZE_CUDA_TRY(cudaMemcpyAsync(s->tb_items.p, items.data(), sizeof(TbItem) * n, cudaMemcpyHostToDevice,
+        if ((rc = s->tb_dirs.ensure(warps * cap)) != BLAZE_OK) return rc;
+        BLAZE_CUDA_TRY(cudaMemcpyAsync(s->tb_items.p, pass_items.data(), sizeof(TbItem) * m, cudaMemcpyHostToDevice,
                                        s->stream));
-        s->stats.h2d_bytes += sizeof(TbItem) * n;
-        for (int attempt = 0;; ++attempt) {
-            if ((rc = s->tb_dirs.ensure(warps * s->tb_dir_cap)) != BLAZE_OK) return rc;
-            TracebackArgs ta{};
-            ta.res = db->d_res;
-            ta.off = db->d_off;
-            ta.q = q->d_q;
-            ta.qlen = q->qlen;
-            ta.items = s->tb_items.p;
-            ta.n_items = static_cast<uint32_t>(n);
-            ta.out = s->tb_out.p;
-            ta.gap_open = p->gap_open;
-            ta.gap_extend = p->gap_extend;
-            ta.xdrop = final_xdrop;
-            ta.dp = s->tb_dp.p;
-            ta.dp_stride = dp_stride;
-            ta.dirs = s->tb_dirs.p;
-            ta.dir_cap = s->tb_dir_cap;
-            ta.rows = s->tb_rows.p;
-            ta.row_cap = row_cap;
-            ta.cursor = s->tb_cursor.p;
-            BLAZE_CUDA_TRY(cudaMemsetAsync(s->tb_cursor.p, 0, sizeof(unsigned long long), s->stream));
-            BLAZE_CUDA_TRY(cudaEventRecord(s->ev[1], s->stream));
-            BLAZE_CUDA_TRY(launch_traceback(ta, blocks, s->stream));
-            BLAZE_CUDA_TRY(cudaEventRecord(s->ev[2], s->stream));
-            s->stats.kernel_launches += 1;
-            BLAZE_CUDA_TRY(cudaMemcpyAsync(outs.data(), s->tb_out.p, sizeof(TbOut) * n, cudaMemcpyDeviceToHost,
-                                           s->stream));
-            BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
-            s->stats.d2h_bytes += sizeof(TbOut) * n;
-            float ms = 0.f;
-            BLAZE_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev[1], s->ev[2]));
-            s->stats.traceback_ms += ms;
-            bool overflow = false;
-            for (const TbOut &o : outs) {
-                s->stats.traceback_cells += static_cast<uint64_t>(o.cells);
-                if (o.status == 2) return BLAZE_ERR_INTERNAL;
-                overflow |= o.status == 1;
-            }
-            if (!overflow) break;
-            if (attempt >= 20) return BLAZE_ERR_LIMIT;
-            s->tb_dir_cap *= 2;  // a longer alignment than the buffers held: again, larger
+        s->stats.h2d_bytes += sizeof(TbItem) * m;
+        TracebackArgs ta{};
+        ta.res = db->d_res;
+        ta.off = db->d_off;
+        ta.q = q->d_q;
+        ta.qlen = q->qlen;
+        ta.items = s->tb_items.p;
+        ta.n_items = static_cast<uint32_t>(m);
+        ta.out = s->tb_out.p;
+        ta.gap_open = p->gap_open;
+        ta.gap_extend = p->gap_extend;
+        ta.xdrop = final_xdrop;
+        ta.dp = s->tb_dp.p;
+        ta.dp_stride = dp_stride;
+        ta.dirs = s->tb_dirs.p;
+        ta.dir_cap = cap;
+        ta.rows = s->tb_rows.p;
+        ta.row_cap = row_cap;
+        ta.cursor = s->tb_cursor.p;
+        BLAZE_CUDA_TRY(cudaMemsetAsync(s->tb_cursor.p, 0, sizeof(unsigned long long), s->stream));
+        BLAZE_CUDA_TRY(cudaEventRecord(s->ev[1], s->stream));
+        BLAZE_CUDA_TRY(launch_traceback(ta, blocks, s->stream));
+        BLAZE_CUDA_TRY(cudaEventRecord(s->ev[2], s->stream));
+        s->stats.kernel_launches += 1;
+        BLAZE_CUDA_TRY(cudaMemcpyAsync(pass_out.data(), s->tb_out.p, sizeof(TbOut) * m, cudaMemcpyDeviceToHost,
+                                       s->stream));
+        BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        s->stats.d2h_bytes += sizeof(TbOut) * m;
+        float ms = 0.f;
+        BLAZE_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev[1], s->ev[2]));
+        s->stats.traceback_ms += ms;
+        std::vector<uint32_t> again;
+        for (size_t k = 0; k < m; ++k) {
+            const TbOut &o = pass_out[k];
+            s->stats.traceback_cells += static_cast<uint64_t>(o.cells);
+            if (o.status == 2) return BLAZE_ERR_INTERNAL;
+            if (o.status == 1) again.push_back(todo[k]);
+            else outs[todo[k]] = o;
         }
+        todo.swap(again);
+        cap *= 4;
     }
     // per subject: purge shared end points, order, E-values, reap
     const double ln2 = std::log(2.0), lnK = std::log(p->K);
