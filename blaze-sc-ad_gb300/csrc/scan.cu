@@ -65,6 +65,43 @@ __device__ __forceinline__ int32_t score_of(uint32_t qa, uint32_t sb) {
     return static_cast<int32_t>(reinterpret_cast<const int8_t *>(smem)[kMatOff + qa * kAlphabet + sb]);
 }
 
+// ------------------------------------------------------------------------
+// Subject staging by the bulk-copy (TMA) engine: one elected lane arms a
+// per-buffer mbarrier with the byte count and issues cp.async.bulk
+// global -> shared; the warp waits on the barrier's phase. Each warp has two
+// stage buffers, so the next subject's copy runs while the current one is
+// scanned. Waits are bounded: a copy that never lands sets kFlagBadState.
+
+constexpr uint32_t kBulkSpinLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_base() { return static_cast<uint32_t>(__cvta_generic_to_shared(smem)); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+
+// Lane 0 of the calling warp: copies `bytes` (a multiple of 16) from 16-byte
+// aligned global `src` to shared offset `dst` and completes the barrier.
+__device__ __forceinline__ void bulk_stage(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    const uint32_t d = smem_base() + dst, b = smem_base() + bar;
+    // earlier generic reads of this buffer come before the async overwrite
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(d), "l"(src), "r"(bytes), "r"(b)
+                 : "memory");
+}
+
 // The subject: staged in shared memory, or read from global memory when it is
 // longer than the staging buffer.
 template <bool STAGED>
@@ -267,6 +304,8 @@ __device__ __forceinline__ int32_t extend_two_hit_warp(const Query<QS> &q, const
 
 struct Finder {
     uint32_t diag, defer, seeds;  // shared offsets
+    uint32_t bars;                // the two stage buffers' mbarriers
+    uint32_t phase;               // bit b: parity the next wait on buffer b expects
     int n_defer, n_seed, sel;
     uint32_t base;
     uint32_t n_init;
@@ -487,27 +526,55 @@ __device__ __forceinline__ unsigned long long scan_subject(Finder &f, const Scan
     return word_hits;
 }
 
-// One subject for the query of `c`: stage it when it fits, find its init
-// hits, and publish them as one contiguous block with a work item.
+constexpr uint32_t kNoStage = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t stage_region(const ScanArgs &a) { return (a.stage_bytes + 32u + 15u) & ~15u; }
+
+// Issues the bulk copy of subject `subj` into stage buffer `buf` when it is
+// long enough to have a word and fits; returns whether it did.
+__device__ __forceinline__ bool stage_issue(const Finder &f, const ScanArgs &a, uint32_t stage, int buf,
+                                            uint32_t subj) {
+    const uint64_t o0 = a.off[subj];
+    const uint64_t slen = a.off[subj + 1] - o0;
+    if (slen < static_cast<uint64_t>(kWordSize) || slen > a.stage_bytes) return false;
+    const uint32_t lead = static_cast<uint32_t>(o0 & 15u);
+    const uint32_t bytes = (lead + static_cast<uint32_t>(slen) + 15u) & ~15u;  // the database is padded
+    if ((threadIdx.x & 31) == 0)
+        bulk_stage(stage + static_cast<uint32_t>(buf) * stage_region(a), a.res + (o0 - lead), bytes,
+                   f.bars + 8u * static_cast<uint32_t>(buf));
+    return true;
+}
+
+// Waits for buffer `buf`'s copy; false (with kFlagBadState set) if it never
+// completes within the spin limit.
+__device__ __forceinline__ bool stage_wait(Finder &f, const ScanArgs &a, int buf) {
+    const uint32_t bar = smem_base() + f.bars + 8u * static_cast<uint32_t>(buf);
+    const uint32_t parity = (f.phase >> buf) & 1u;
+    for (uint32_t i = 0; i < kBulkSpinLimit; ++i) {
+        if (mbar_try_wait(bar, parity)) {
+            f.phase ^= 1u << buf;
+            return true;
+        }
+    }
+    if ((threadIdx.x & 31) == 0) atomicOr(&a.cnt->flags, kFlagBadState);
+    return false;
+}
+
+// One subject for the query of `c` (staged at shared offset `staged` by a
+// bulk copy, or read from global memory): find its init hits and publish
+// them as one contiguous block with a work item.
 template <bool QS, bool PSMEM>
 __device__ __forceinline__ void process_subject(Finder &f, const ScanArgs &a, const Ctx &c, const Query<QS> &q,
-                                                uint32_t subj, uint32_t query_index, uint32_t stage,
+                                                uint32_t subj, uint32_t query_index, uint32_t staged,
                                                 unsigned long long &word_hits, unsigned long long &residues) {
     const int lane = threadIdx.x & 31;
     const uint64_t o0 = a.off[subj];
     const int32_t slen = static_cast<int32_t>(a.off[subj + 1] - o0);
     f.n_init = 0;
     residues += static_cast<unsigned long long>(slen);
-    if (static_cast<uint32_t>(slen) <= a.stage_bytes) {
-        // stage the subject: 16-byte aligned vectors covering it (the
-        // database is padded, so the last vector stays in bounds)
-        const uint32_t lead = static_cast<uint32_t>(o0 & 15u);
-        const uint4 *src = reinterpret_cast<const uint4 *>(a.res + (o0 - lead));
-        const uint32_t nvec = (lead + static_cast<uint32_t>(slen) + 15u) >> 4;
-        for (uint32_t i = lane; i < nvec; i += 32) reinterpret_cast<uint4 *>(smem)[(stage >> 4) + i] = __ldg(src + i);
-        __syncwarp();
+    if (staged != kNoStage) {
         Subject<true> sub;
-        sub.off = stage + lead;
+        sub.off = staged + static_cast<uint32_t>(o0 & 15u);
         sub.ptr = nullptr;
         sub.len = slen;
         word_hits += scan_subject<QS, true, PSMEM>(f, a, c, q, sub);
@@ -566,7 +633,14 @@ __device__ __forceinline__ Finder make_finder(const ScanArgs &a, uint32_t qbytes
     f.diag = mine;
     f.defer = mine + a.diag_bytes;
     f.seeds = f.defer + 2u * kDeferCap * sizeof(uint2);
-    stage = f.seeds + kSeedCap * sizeof(int4);
+    f.bars = f.seeds + kSeedCap * sizeof(int4);  // two 8-byte mbarriers, 16 bytes
+    stage = f.bars + 16u;                         // two stage buffers of stage_region bytes
+    f.phase = 0u;
+    if (lane == 0) {
+        mbar_init(smem_base() + f.bars);
+        mbar_init(smem_base() + f.bars + 8u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     f.n_defer = f.n_seed = f.sel = 0;
     f.base = 0;
     f.extensions = 0;
@@ -616,12 +690,18 @@ scan_kernel(const ScanArgs a) {
     q.ptr = a.q;
     q.len = a.qlen;
     unsigned long long word_hits = 0, residues = 0;
-    for (;;) {
+    const unsigned long long count = a.n_subj;
+    auto next = [&]() {
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(a.cursor, 1ull);
-        t = __shfl_sync(kFull, t, 0);
-        if (t >= a.n_subj) break;
-        process_subject<QS, true>(f, a, c, q, a.n_subj - 1 - static_cast<uint32_t>(t), 0u, stage, word_hits, residues);
+        return __shfl_sync(kFull, t, 0);
+    };
+    // subjects longest first, each staged by a bulk copy when it fits
+    for (unsigned long long t = next(); t < count; t = next()) {
+        const uint32_t subj = a.n_subj - 1 - static_cast<uint32_t>(t);
+        const bool staged = stage_issue(f, a, stage, 0, subj);
+        if (staged && !stage_wait(f, a, 0)) return;
+        process_subject<QS, true>(f, a, c, q, subj, 0u, staged ? stage : kNoStage, word_hits, residues);
     }
     finish_counters(a, f, word_hits, residues);
 }
@@ -666,8 +746,12 @@ scan_batch_kernel(const ScanArgs a) {
         q.ptr = bq.q;
         q.len = bq.qlen;
         const uint32_t hi = a.tile_bounds[range], lo = a.tile_bounds[range + 1];
-        for (uint32_t subj = hi; subj-- > lo;)
-            process_subject<false, false>(f, a, c, q, subj, bq.index, stage, word_hits, residues);
+        for (uint32_t subj = hi; subj-- > lo;) {
+            const bool staged = stage_issue(f, a, stage, 0, subj);
+            if (staged && !stage_wait(f, a, 0)) return;
+            process_subject<false, false>(f, a, c, q, subj, bq.index, staged ? stage : kNoStage, word_hits,
+                                          residues);
+        }
     }
     finish_counters(a, f, word_hits, residues);
 }
@@ -681,7 +765,7 @@ ScanLayout scan_layout(int32_t qlen, int32_t window, uint32_t stage_bytes, size_
     l.diag_bytes = l.diag_entries * 4u;
     l.stage_bytes = stage_bytes;
     l.query_smem_bytes = qlen <= kQuerySmemMax ? (static_cast<uint32_t>(qlen) + 15u) & ~15u : 0u;
-    l.warp_smem_bytes = l.diag_bytes + 2 * kDeferCap * sizeof(uint2) + kSeedCap * sizeof(int4) +
+    l.warp_smem_bytes = l.diag_bytes + 2 * kDeferCap * sizeof(uint2) + kSeedCap * sizeof(int4) + 16u +
                         ((stage_bytes + 32u + 15u) & ~15u);
     const size_t fixed = kScanMatBytes + kScanPresenceBytes + l.query_smem_bytes;
     int w = std::max(1, std::min(max_warps, kScanMaxWarpsPerBlock));
