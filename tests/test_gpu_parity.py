@@ -165,3 +165,23 @@ def test_hitlist_culling(cull):
         assert len(set(got["oid"].tolist())) == min(cull["hitlist_size"], len(set(full["oid"].tolist())))
     if "max_hsps" in cull:
         assert np.bincount(got["oid"]).max() <= cull["max_hsps"]
+
+
+def test_stage_boundary_subjects():
+    # subjects around the staging bound (1,024 residues: longer ones are read
+    # from global memory) at every 16-byte alignment of their start
+    rng = np.random.default_rng(1024)
+    q = synth.random_residues(rng, 350)
+    seqs = []
+    for k, L in enumerate((1008, 1016, 1020, 1023, 1024, 1025, 1040, 2047, 2048, 2049) * 4):
+        s = synth.random_residues(rng, L)
+        w = int(rng.integers(60, 200))
+        s0 = int(rng.integers(0, len(q) - w))
+        pos = int(rng.integers(0, L - w))
+        s[pos:pos + w] = synth.mutate(rng, q[s0:s0 + w], 0.6)[:w] if len(synth.mutate(rng, q[s0:s0 + w], 0.6)) >= w \
+            else s[pos:pos + w]
+        seqs.append(s)
+        seqs.append(synth.random_residues(rng, 1 + k % 15))  # shifts the next start's alignment
+    res, off = concat(seqs)
+    got, _, _ = compare(q, res, off)
+    assert len(got) > 5
