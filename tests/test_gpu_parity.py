@@ -178,8 +178,8 @@ def test_stage_boundary_subjects():
         w = int(rng.integers(60, 200))
         s0 = int(rng.integers(0, len(q) - w))
         pos = int(rng.integers(0, L - w))
-        s[pos:pos + w] = synth.mutate(rng, q[s0:s0 + w], 0.6)[:w] if len(synth.mutate(rng, q[s0:s0 + w], 0.6)) >= w \
-            else s[pos:pos + w]
+        hom = synth.mutate(rng, q[s0:s0 + w], 0.6)[:w]  # a homologous stretch, length kept
+        s[pos:pos + len(hom)] = hom
         seqs.append(s)
         seqs.append(synth.random_residues(rng, 1 + k % 15))  # shifts the next start's alignment
     res, off = concat(seqs)
