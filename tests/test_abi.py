@@ -78,3 +78,56 @@ def test_no_device_is_reported_not_faked(lib):
     assert st == 3  # BLAZE_ERR_NO_DEVICE
     with pytest.raises(blaze103.BlazeError):
         blaze103.SeqSrc(res, off)
+
+
+C_CLIENT = r"""
+#include <stdio.h>
+#include "blaze_prelim.h"
+
+/* A plain C client of the ABI: the header must compile as C99 and the
+ * library link from C. Only calls that need no GPU run here. */
+int main(void) {
+    blaze_params p;
+    int n = 0;
+    if (blaze_params_default(300, 7000000ull, 20000u, 10.0, &p) != BLAZE_OK) return 1;
+    blaze_device_count(&n);
+    printf("%d %d %d %d %d %s\n", p.gapped_cutoff, p.ungapped_cutoff, p.window, p.gapped_xdrop,
+           p.hitlist_size, blaze_status_string(BLAZE_ERR_OUTPUT_TOO_SMALL));
+    /* every entry point is referenced, so the link checks them all */
+    void *fns[] = {(void *)blaze_db_create, (void *)blaze_db_free, (void *)blaze_db_info,
+                   (void *)blaze_query_create, (void *)blaze_query_free, (void *)blaze_search_create,
+                   (void *)blaze_search_free, (void *)blaze_search_run, (void *)blaze_search_results,
+                   (void *)blaze_search_stats, (void *)blaze_search_init_hits, (void *)blaze_prelim_search,
+                   (void *)blaze_batch_create, (void *)blaze_batch_free, (void *)blaze_batch_info,
+                   (void *)blaze_search_run_batch, (void *)blaze_search_batch_results,
+                   (void *)blaze_search_set_tuning, (void *)blaze_search_traceback,
+                   (void *)blaze_search_traceback_results, (void *)blaze_server_create,
+                   (void *)blaze_server_submit, (void *)blaze_server_wait, (void *)blaze_server_take,
+                   (void *)blaze_server_stats_get, (void *)blaze_server_free, (void *)blaze_volume_info,
+                   (void *)blaze_volume_read, (void *)blaze_db_open, (void *)blaze_gapped_noalloc,
+                   (void *)blaze_last_cuda_error};
+    return fns[0] == 0;
+}
+"""
+
+
+def test_header_compiles_and_links_from_c(lib, tmp_path):
+    import shutil
+    import subprocess
+
+    import blaze103
+    import oracle
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "client.c"
+    src.write_text(C_CLIENT)
+    exe = tmp_path / "client"
+    libdir = os.path.dirname(blaze103._lib.LIB_PATH)
+    cmd = ["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"), str(src),
+           "-L", libdir, "-lblaze103", f"-Wl,-rpath,{libdir}", "-o", str(exe)]
+    subprocess.run(cmd, check=True, capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    o = oracle.default_params(300, 7_000_000, 20_000)
+    assert [int(x) for x in out[:5]] == [o["gapped_cutoff"], o["ungapped_cutoff"], 40, 38, 0]
+    assert "output" in " ".join(out[5:])
