@@ -383,3 +383,6 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+from . import shard, tabular, volume  # noqa: E402,F401  (submodules of the public API)

@@ -185,3 +185,27 @@ def test_stage_boundary_subjects():
     res, off = concat(seqs)
     got, _, _ = compare(q, res, off)
     assert len(got) > 5
+
+
+def test_sharded_search_one_rank_matches_plain(tmp_path):
+    # the sharding glue (partition, offsets into the shared residue array,
+    # global statistics, gather and merge) on one rank over gloo
+    import torch.distributed as dist
+
+    from blaze103 import shard
+
+    w = synth.make_workload("plain-small", scale=0.05)
+    store = dist.FileStore(str(tmp_path / "store"), 1)
+    dist.init_process_group("gloo", store=store, rank=0, world_size=1)
+    try:
+        merged = shard.sharded_search(w.residues, w.offsets, w.queries)
+    finally:
+        dist.destroy_process_group()
+    db = blaze103.SeqSrc(w.residues, w.offsets)
+    ps = blaze103.PrelimSearch(db)
+    for q, got in zip(w.queries, merged):
+        want = ps.run(q).hsps
+        for f in blaze103.HSP_DTYPE.names:
+            assert np.array_equal(got[f], want[f]), f
+    ps.close()
+    db.close()
