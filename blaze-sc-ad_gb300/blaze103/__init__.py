@@ -25,11 +25,11 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import (ALIGNED_DTYPE, BATCH_HSP_DTYPE, HSP_DTYPE, INIT_DTYPE, BlazeError, BlazeParams, BlazeServerConfig,
+from ._lib import (ALIGNED_DTYPE, BATCH_ALIGNED_DTYPE, BATCH_HSP_DTYPE, HSP_DTYPE, INIT_DTYPE, BlazeError, BlazeParams, BlazeServerConfig,
                    BlazeServerStats, BlazeStats, BlazeTuning, check, load, u8ptr, u64ptr, status_string)
 
 __all__ = ["SeqSrc", "PrelimSearch", "HSPResults", "QueryBatch", "Server", "BlazeParams", "BlazeTuning",
-           "BlazeError", "HSP_DTYPE", "BATCH_HSP_DTYPE", "ALIGNED_DTYPE", "default_params", "device_count", "load",
+           "BlazeError", "HSP_DTYPE", "BATCH_HSP_DTYPE", "ALIGNED_DTYPE", "BATCH_ALIGNED_DTYPE", "default_params", "device_count", "load",
            "status_string"]
 
 
@@ -303,6 +303,20 @@ class PrelimSearch:
             return out[: n.value]
         finally:
             q.close()
+
+    def traceback_batch(self, batch: QueryBatch, params, evalue: float | None = None,
+                        final_xdrop: int = 64) -> np.ndarray:
+        """Traceback stage over the last batched run (which must have searched
+        `batch` with `params`): BATCH_ALIGNED_DTYPE records by query, then OID."""
+        arr = (BlazeParams * len(params))(*params)
+        ev = params[0].prelim_evalue if evalue is None else float(evalue)
+        n = ctypes.c_uint64()
+        check(self._lib.blaze_search_traceback_batch(self._h, batch.handle, arr, int(final_xdrop), ev,
+                                                     ctypes.byref(n)), "blaze_search_traceback_batch")
+        out = np.zeros(n.value, dtype=BATCH_ALIGNED_DTYPE)
+        check(self._lib.blaze_search_traceback_batch_results(self._h, out.ctypes.data_as(ctypes.c_void_p), n.value,
+                                                             ctypes.byref(n)), "blaze_search_traceback_batch_results")
+        return out[: n.value]
 
     def prelim_search(self, query, params: BlazeParams, capacity: int) -> np.ndarray:
         """The one-call C-ABI path with host buffers (blaze_prelim_search)."""

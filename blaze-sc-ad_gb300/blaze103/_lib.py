@@ -20,7 +20,8 @@ EXPORTS = (
     "blaze_search_batch_results", "blaze_search_set_tuning",
     "blaze_server_create", "blaze_server_submit", "blaze_server_wait", "blaze_server_take",
     "blaze_server_stats_get", "blaze_server_free", "blaze_volume_info", "blaze_volume_read", "blaze_db_open",
-    "blaze_search_traceback", "blaze_search_traceback_results",
+    "blaze_search_traceback", "blaze_search_traceback_results", "blaze_search_traceback_batch",
+    "blaze_search_traceback_batch_results",
 )
 
 HSP_DTYPE = np.dtype([
@@ -38,6 +39,9 @@ ALIGNED_DTYPE = np.dtype([
     ("gap_opens", "<i4"), ("gaps", "<i4"), ("reserved", "<i4"), ("evalue", "<f8"), ("bit_score", "<f8"),
 ], align=True)
 assert ALIGNED_DTYPE.itemsize == 72
+BATCH_ALIGNED_DTYPE = np.dtype([("query", "<u4"), ("pad", "<u4")] + [
+    (n, ALIGNED_DTYPE.fields[n][0]) for n in ALIGNED_DTYPE.names], align=True)
+assert BATCH_ALIGNED_DTYPE.itemsize == 80 and BATCH_ALIGNED_DTYPE.fields["evalue"][1] == 64
 INIT_DTYPE = np.dtype([
     ("oid", "<u4"), ("q_start", "<i4"), ("s_start", "<i4"), ("length", "<i4"), ("score", "<i4"),
     ("q_trigger", "<i4"), ("s_trigger", "<i4"),
@@ -166,6 +170,8 @@ def load(path: str | None = None):
     L.blaze_db_open.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.POINTER(vp)]
     L.blaze_search_traceback.argtypes = [vp, vp, ctypes.POINTER(BlazeParams), i32, ctypes.c_double, u64p]
     L.blaze_search_traceback_results.argtypes = [vp, vp, ctypes.c_uint64, u64p]
+    L.blaze_search_traceback_batch.argtypes = [vp, vp, ctypes.POINTER(BlazeParams), i32, ctypes.c_double, u64p]
+    L.blaze_search_traceback_batch_results.argtypes = [vp, vp, ctypes.c_uint64, u64p]
     for name in EXPORTS:
         if name not in ("blaze_status_string", "blaze_last_cuda_error"):
             getattr(L, name).restype = ctypes.c_int

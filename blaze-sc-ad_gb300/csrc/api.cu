@@ -124,6 +124,8 @@ struct blaze_search {
     DevBuf<unsigned long long> tb_cursor;
     unsigned long long tb_dir_cap = 1ull << 16;  // direction bytes per warp in a first pass
     std::vector<blaze_aligned_hsp> tb_results;
+    std::vector<blaze_batch_aligned_hsp> tb_batch_results;
+    const blaze_batch *last_batch = nullptr;  // the batch of the last batched run
 };
 
 struct blaze_batch {
@@ -908,6 +910,7 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
     s->last_init_count = c.init_count;
     s->last_work_count = c.work_count;
     s->last_batched = batched;
+    s->last_batch = r.b;
     s->stats.residues_scanned = c.residues;
     s->stats.word_hits = c.word_hits;
     s->stats.ungapped_extensions = c.extensions;
@@ -1192,40 +1195,28 @@ extern "C" int blaze_prelim_search(blaze_search *s, const uint8_t *query, int32_
 // ------------------------------------------------------------------------
 // Traceback stage.
 
-extern "C" int blaze_search_traceback(blaze_search *s, const blaze_query *q, const blaze_params *p,
-                                      int32_t final_xdrop, double evalue, uint64_t *n_hsps) {
-    if (!s || !q || !p || final_xdrop <= 0 || q->device != s->db->device || s->last_batched)
-        return BLAZE_ERR_INVALID_ARG;
-    int rc = check_params(p);
-    if (rc != BLAZE_OK) return rc;
-    if (n_hsps) *n_hsps = 0;
-    s->tb_results.clear();
-    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
+// Traces `items` in passes: the first over all of them with many warps and
+// small direction buffers, the next ones over those whose alignment did not
+// fit, with fewer warps and buffers four times larger. `q`/`qlen` is the
+// query of a single-query run; `batch_q`/`batch_qlen` (device arrays) the
+// queries of a batched run, indexed by TbItem::query.
+static int traceback_passes(blaze_search *s, const std::vector<TbItem> &items, const blaze_params *p,
+                            int32_t final_xdrop, const uint8_t *q, int32_t qlen, const uint8_t *const *batch_q,
+                            const int32_t *batch_qlen, int32_t max_qlen, std::vector<TbOut> &outs) {
     const blaze_db *db = s->db;
-    const size_t n = s->results.size();
-    std::vector<TbItem> items(n);
-    for (size_t i = 0; i < n; ++i) {
-        const blaze_hsp &h = s->results[i];
-        if (h.oid >= db->n || h.q_gapped_start < 0 || h.q_gapped_start >= q->qlen) return BLAZE_ERR_INVALID_ARG;
-        const uint32_t sub = db->sorted_of[h.oid];
-        if (h.s_gapped_start < 0 || static_cast<uint64_t>(h.s_gapped_start) >= db->h_off[sub + 1] - db->h_off[sub])
-            return BLAZE_ERR_INVALID_ARG;
-        items[i] = TbItem{sub, h.q_gapped_start, h.s_gapped_start, 0u};
-    }
-    std::vector<TbOut> outs(n);
+    const size_t n = items.size();
+    outs.assign(n, TbOut{});
     s->stats.traceback_ms = 0.f;
     s->stats.traceback_hsps = static_cast<uint32_t>(n);
     s->stats.traceback_cells = 0;
-    // Passes over the HSPs still to trace: the first over all of them with
-    // many warps and small direction buffers, the next ones over those whose
-    // alignment did not fit, with fewer warps and buffers four times larger.
     std::vector<uint32_t> todo(n);
     for (size_t i = 0; i < n; ++i) todo[i] = static_cast<uint32_t>(i);
     unsigned long long cap = s->tb_dir_cap;
-    const uint32_t row_cap = static_cast<uint32_t>(q->qlen) + 2u;
+    const uint32_t row_cap = static_cast<uint32_t>(max_qlen) + 2u;
     const uint32_t dp_stride = std::max<uint32_t>(db->max_len, 1u) + 2u;
     std::vector<TbItem> pass_items;
     std::vector<TbOut> pass_out;
+    int rc;
     for (int attempt = 0; !todo.empty(); ++attempt) {
         if (attempt > 12) return BLAZE_ERR_LIMIT;
         const size_t m = todo.size();
@@ -1247,8 +1238,10 @@ extern "C" int blaze_search_traceback(blaze_search *s, const blaze_query *q, con
         TracebackArgs ta{};
         ta.res = db->d_res;
         ta.off = db->d_off;
-        ta.q = q->d_q;
-        ta.qlen = q->qlen;
+        ta.q = q;
+        ta.qlen = qlen;
+        ta.batch_q = batch_q;
+        ta.batch_qlen = batch_qlen;
         ta.items = s->tb_items.p;
         ta.n_items = static_cast<uint32_t>(m);
         ta.out = s->tb_out.p;
@@ -1285,63 +1278,150 @@ extern "C" int blaze_search_traceback(blaze_search *s, const blaze_query *q, con
         todo.swap(again);
         cap *= 4;
     }
-    // per subject: purge shared end points, order, E-values, reap
-    const double ln2 = std::log(2.0), lnK = std::log(p->K);
+    return BLAZE_OK;
+}
+
+// One subject's traced HSPs: purged of shared start and end points (the
+// better kept), ordered as the preliminary stage orders them, given final
+// E-values and bit scores and reaped at `evalue`; appended to `out`.
+static void traceback_finish_subject(std::vector<TbOut> g, uint32_t oid, const blaze_params &p, double evalue,
+                                     std::vector<blaze_aligned_hsp> &out) {
+    auto by_start = [](const TbOut &a, const TbOut &b) {
+        if (a.q_start != b.q_start) return a.q_start < b.q_start;
+        if (a.s_start != b.s_start) return a.s_start < b.s_start;
+        if (a.score != b.score) return a.score > b.score;
+        if (a.q_end != b.q_end) return a.q_end > b.q_end;
+        return a.s_end > b.s_end;
+    };
+    auto by_end = [](const TbOut &a, const TbOut &b) {
+        if (a.q_end != b.q_end) return a.q_end < b.q_end;
+        if (a.s_end != b.s_end) return a.s_end < b.s_end;
+        if (a.score != b.score) return a.score > b.score;
+        if (a.q_start != b.q_start) return a.q_start < b.q_start;
+        return a.s_start < b.s_start;
+    };
+    auto by_score = [](const TbOut &a, const TbOut &b) {
+        if (a.score != b.score) return a.score > b.score;
+        if (a.s_start != b.s_start) return a.s_start < b.s_start;
+        if (a.s_end != b.s_end) return a.s_end > b.s_end;
+        if (a.q_start != b.q_start) return a.q_start < b.q_start;
+        return a.q_end > b.q_end;
+    };
+    std::stable_sort(g.begin(), g.end(), by_start);
+    std::vector<TbOut> m;
+    for (const TbOut &o : g)
+        if (m.empty() || o.q_start != m.back().q_start || o.s_start != m.back().s_start) m.push_back(o);
+    std::stable_sort(m.begin(), m.end(), by_end);
+    std::vector<TbOut> m2;
+    for (const TbOut &o : m)
+        if (m2.empty() || o.q_end != m2.back().q_end || o.s_end != m2.back().s_end) m2.push_back(o);
+    std::stable_sort(m2.begin(), m2.end(), by_score);
+    const double ln2 = std::log(2.0), lnK = std::log(p.K);
+    for (const TbOut &o : m2) {
+        blaze_aligned_hsp h{};
+        h.oid = oid;
+        h.score = o.score;
+        h.q_start = o.q_start;
+        h.q_end = o.q_end;
+        h.s_start = o.s_start;
+        h.s_end = o.s_end;
+        h.length = o.length;
+        h.identities = o.identities;
+        h.positives = o.positives;
+        h.mismatches = o.mismatches;
+        h.gap_opens = o.gap_opens;
+        h.gaps = o.gaps;
+        h.evalue = p.eff_searchsp * p.K * std::exp(-p.lambda * static_cast<double>(o.score));
+        h.bit_score = (p.lambda * static_cast<double>(o.score) - lnK) / ln2;
+        if (h.evalue <= evalue) out.push_back(h);
+    }
+}
+
+static int tb_item(const blaze_db *db, const blaze_hsp &h, int32_t qlen, uint32_t query, TbItem *it) {
+    if (h.oid >= db->n || h.q_gapped_start < 0 || h.q_gapped_start >= qlen) return BLAZE_ERR_INVALID_ARG;
+    const uint32_t sub = db->sorted_of[h.oid];
+    if (h.s_gapped_start < 0 || static_cast<uint64_t>(h.s_gapped_start) >= db->h_off[sub + 1] - db->h_off[sub])
+        return BLAZE_ERR_INVALID_ARG;
+    *it = TbItem{sub, h.q_gapped_start, h.s_gapped_start, query};
+    return BLAZE_OK;
+}
+
+extern "C" int blaze_search_traceback(blaze_search *s, const blaze_query *q, const blaze_params *p,
+                                      int32_t final_xdrop, double evalue, uint64_t *n_hsps) {
+    if (!s || !q || !p || final_xdrop <= 0 || q->device != s->db->device || s->last_batched)
+        return BLAZE_ERR_INVALID_ARG;
+    int rc = check_params(p);
+    if (rc != BLAZE_OK) return rc;
+    if (n_hsps) *n_hsps = 0;
+    s->tb_results.clear();
+    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
+    const size_t n = s->results.size();
+    std::vector<TbItem> items(n);
+    for (size_t i = 0; i < n; ++i)
+        if ((rc = tb_item(s->db, s->results[i], q->qlen, 0u, &items[i])) != BLAZE_OK) return rc;
+    std::vector<TbOut> outs;
+    if ((rc = traceback_passes(s, items, p, final_xdrop, q->d_q, q->qlen, nullptr, nullptr, q->qlen, outs)) !=
+        BLAZE_OK)
+        return rc;
     for (size_t i = 0; i < n;) {
         size_t j = i;
         while (j < n && s->results[j].oid == s->results[i].oid) ++j;
-        std::vector<TbOut> g(outs.begin() + i, outs.begin() + j);
-        auto by_start = [](const TbOut &a, const TbOut &b) {
-            if (a.q_start != b.q_start) return a.q_start < b.q_start;
-            if (a.s_start != b.s_start) return a.s_start < b.s_start;
-            if (a.score != b.score) return a.score > b.score;
-            if (a.q_end != b.q_end) return a.q_end > b.q_end;
-            return a.s_end > b.s_end;
-        };
-        auto by_end = [](const TbOut &a, const TbOut &b) {
-            if (a.q_end != b.q_end) return a.q_end < b.q_end;
-            if (a.s_end != b.s_end) return a.s_end < b.s_end;
-            if (a.score != b.score) return a.score > b.score;
-            if (a.q_start != b.q_start) return a.q_start < b.q_start;
-            return a.s_start < b.s_start;
-        };
-        auto by_score = [](const TbOut &a, const TbOut &b) {
-            if (a.score != b.score) return a.score > b.score;
-            if (a.s_start != b.s_start) return a.s_start < b.s_start;
-            if (a.s_end != b.s_end) return a.s_end > b.s_end;
-            if (a.q_start != b.q_start) return a.q_start < b.q_start;
-            return a.q_end > b.q_end;
-        };
-        std::stable_sort(g.begin(), g.end(), by_start);
-        std::vector<TbOut> m;
-        for (const TbOut &o : g)
-            if (m.empty() || o.q_start != m.back().q_start || o.s_start != m.back().s_start) m.push_back(o);
-        std::stable_sort(m.begin(), m.end(), by_end);
-        std::vector<TbOut> m2;
-        for (const TbOut &o : m)
-            if (m2.empty() || o.q_end != m2.back().q_end || o.s_end != m2.back().s_end) m2.push_back(o);
-        std::stable_sort(m2.begin(), m2.end(), by_score);
-        for (const TbOut &o : m2) {
-            blaze_aligned_hsp h{};
-            h.oid = s->results[i].oid;
-            h.score = o.score;
-            h.q_start = o.q_start;
-            h.q_end = o.q_end;
-            h.s_start = o.s_start;
-            h.s_end = o.s_end;
-            h.length = o.length;
-            h.identities = o.identities;
-            h.positives = o.positives;
-            h.mismatches = o.mismatches;
-            h.gap_opens = o.gap_opens;
-            h.gaps = o.gaps;
-            h.evalue = p->eff_searchsp * p->K * std::exp(-p->lambda * static_cast<double>(o.score));
-            h.bit_score = (p->lambda * static_cast<double>(o.score) - lnK) / ln2;
-            if (h.evalue <= evalue) s->tb_results.push_back(h);
-        }
+        traceback_finish_subject(std::vector<TbOut>(outs.begin() + i, outs.begin() + j), s->results[i].oid, *p,
+                                 evalue, s->tb_results);
         i = j;
     }
     if (n_hsps) *n_hsps = s->tb_results.size();
+    return BLAZE_OK;
+}
+
+extern "C" int blaze_search_traceback_batch(blaze_search *s, const blaze_batch *b, const blaze_params *params,
+                                            int32_t final_xdrop, double evalue, uint64_t *n_hsps) {
+    if (!s || !b || !params || final_xdrop <= 0 || !s->last_batched || s->last_batch != b)
+        return BLAZE_ERR_INVALID_ARG;
+    int rc;
+    for (uint32_t i = 0; i < b->n; ++i)
+        if ((rc = check_params(&params[i])) != BLAZE_OK) return rc;
+    if (n_hsps) *n_hsps = 0;
+    s->tb_batch_results.clear();
+    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
+    const size_t n = s->batch_results.size();
+    std::vector<TbItem> items(n);
+    int32_t max_qlen = 1;
+    for (uint32_t i = 0; i < b->n; ++i) max_qlen = std::max(max_qlen, b->qlen[i]);
+    for (size_t i = 0; i < n; ++i) {
+        const blaze_batch_hsp &bh = s->batch_results[i];
+        if (bh.query >= b->n) return BLAZE_ERR_INVALID_ARG;
+        if ((rc = tb_item(s->db, bh.hsp, b->qlen[bh.query], bh.query, &items[i])) != BLAZE_OK) return rc;
+    }
+    // the per-query arrays of the last batched run (batch order) are still
+    // on the device
+    std::vector<TbOut> outs;
+    if ((rc = traceback_passes(s, items, &params[0], final_xdrop, nullptr, 0, s->bqptr.p, s->bqlen.p, max_qlen,
+                               outs)) != BLAZE_OK)
+        return rc;
+    std::vector<blaze_aligned_hsp> one;
+    for (size_t i = 0; i < n;) {
+        size_t j = i;
+        const uint32_t qi = s->batch_results[i].query, oid = s->batch_results[i].hsp.oid;
+        while (j < n && s->batch_results[j].query == qi && s->batch_results[j].hsp.oid == oid) ++j;
+        one.clear();
+        traceback_finish_subject(std::vector<TbOut>(outs.begin() + i, outs.begin() + j), oid, params[qi], evalue,
+                                 one);
+        for (const blaze_aligned_hsp &h : one) s->tb_batch_results.push_back(blaze_batch_aligned_hsp{qi, 0u, h});
+        i = j;
+    }
+    if (n_hsps) *n_hsps = s->tb_batch_results.size();
+    return BLAZE_OK;
+}
+
+extern "C" int blaze_search_traceback_batch_results(const blaze_search *s, blaze_batch_aligned_hsp *out,
+                                                    uint64_t capacity, uint64_t *n_hsps) {
+    if (!s) return BLAZE_ERR_INVALID_ARG;
+    const size_t n = s->tb_batch_results.size();
+    if (n_hsps) *n_hsps = n;
+    if (capacity < n) return BLAZE_ERR_OUTPUT_TOO_SMALL;
+    if (n && !out) return BLAZE_ERR_INVALID_ARG;
+    if (n) std::memcpy(out, s->tb_batch_results.data(), sizeof(blaze_batch_aligned_hsp) * n);
     return BLAZE_OK;
 }
 

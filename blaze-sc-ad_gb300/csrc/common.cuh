@@ -149,7 +149,7 @@ struct ScanLayout {
 struct TbItem {
     uint32_t subject;  // index into the length-sorted database
     int32_t q_off, s_off;
-    uint32_t pad;
+    uint32_t query;    // batched runs: the query's position in its batch
 };
 
 struct TbOut {
@@ -164,6 +164,8 @@ struct TracebackArgs {
     const uint64_t *off;
     const uint8_t *q;
     int32_t qlen;
+    const uint8_t *const *batch_q;  // batched runs: per query (q, qlen unused)
+    const int32_t *batch_qlen;
     const TbItem *items;
     uint32_t n_items;
     TbOut *out;

@@ -296,19 +296,21 @@ __global__ void __launch_bounds__(kTracebackWarpsPerBlock * 32) traceback_kernel
         const uint8_t *sub = a.res + o0;
         const int32_t slen = static_cast<int32_t>(a.off[it.subject + 1] - o0);
         const int32_t q_off = it.q_off, s_off = it.s_off;
+        const uint8_t *qres = a.batch_q ? a.batch_q[it.query] : a.q;
+        const int32_t qlen = a.batch_q ? a.batch_qlen[it.query] : a.qlen;
         d.overflow = false;
         int32_t al, bl, ar = 0, br = 0, right = 0, rows, cells = 0;
         TbOut o{};
-        const int32_t left = xdrop_dp_dirs<true>(a.q, sub, q_off + 1, s_off + 1, a.gap_open, a.gap_extend, a.xdrop,
+        const int32_t left = xdrop_dp_dirs<true>(qres, sub, q_off + 1, s_off + 1, a.gap_open, a.gap_extend, a.xdrop,
                                                  mat, Hb, Eb, &al, &bl, d, &rows, &cells);
         Walk wl{0, 0, 0, 0, 0, -1, true}, wr{0, 0, 0, 0, 0, -1, true};
-        if (!d.overflow && lane == 0) wl = walk_back<true>(d, rows, a.q, sub, q_off + 1, s_off + 1, al, bl, mat);
+        if (!d.overflow && lane == 0) wl = walk_back<true>(d, rows, qres, sub, q_off + 1, s_off + 1, al, bl, mat);
         __syncwarp();
-        if (!d.overflow && q_off < a.qlen - 1 && s_off < slen - 1) {
-            right = xdrop_dp_dirs<false>(a.q + q_off, sub + s_off, a.qlen - q_off - 1, slen - s_off - 1, a.gap_open,
+        if (!d.overflow && q_off < qlen - 1 && s_off < slen - 1) {
+            right = xdrop_dp_dirs<false>(qres + q_off, sub + s_off, qlen - q_off - 1, slen - s_off - 1, a.gap_open,
                                          a.gap_extend, a.xdrop, mat, Hb, Eb, &ar, &br, d, &rows, &cells);
             if (!d.overflow && lane == 0)
-                wr = walk_back<false>(d, rows, a.q + q_off, sub + s_off, a.qlen - q_off - 1, slen - s_off - 1, ar,
+                wr = walk_back<false>(d, rows, qres + q_off, sub + s_off, qlen - q_off - 1, slen - s_off - 1, ar,
                                       br, mat);
         }
         if (lane == 0) {

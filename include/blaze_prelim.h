@@ -48,6 +48,7 @@ typedef enum blaze_status {
 typedef struct blaze_db blaze_db;         /* resident residue database */
 typedef struct blaze_query blaze_query;   /* query + word lookup on the device */
 typedef struct blaze_search blaze_search; /* stream, scratch and results */
+typedef struct blaze_batch blaze_batch;   /* many queries' tables on the device */
 
 /* Search parameters. Raw scores; NCBI BLAST defaults for BLOSUM62 11/1 are
  * word_threshold 11, window 40, ungapped_xdrop 16, gap_open 11,
@@ -207,6 +208,18 @@ int blaze_search_traceback(blaze_search *s, const blaze_query *q, const blaze_pa
 int blaze_search_traceback_results(const blaze_search *s, blaze_aligned_hsp *out, uint64_t capacity,
                                    uint64_t *n_hsps);
 
+/* The same for the last batched run of s, which must have searched b with
+ * `params` (one set per query): records by query, then OID. */
+typedef struct blaze_batch_aligned_hsp {
+    uint32_t query;
+    uint32_t reserved;
+    blaze_aligned_hsp hsp;
+} blaze_batch_aligned_hsp;
+int blaze_search_traceback_batch(blaze_search *s, const blaze_batch *b, const blaze_params *params,
+                                 int32_t final_xdrop, double evalue, uint64_t *n_hsps);
+int blaze_search_traceback_batch_results(const blaze_search *s, blaze_batch_aligned_hsp *out, uint64_t capacity,
+                                         uint64_t *n_hsps);
+
 /* ---------------------------------------------------------------------
  * Batched form: many queries of uneven length against the database in one
  * persistent launch per stage. Warps pull (query, subject range) tiles from a
@@ -214,7 +227,6 @@ int blaze_search_traceback_results(const blaze_search *s, blaze_aligned_hsp *out
  * queries of a batch share word_threshold, window, X-drops and gap costs;
  * cutoffs and E-value statistics are per query (params[i]).
  */
-typedef struct blaze_batch blaze_batch;
 
 /* One HSP of a batched run: the query's index in the batch and the HSP. */
 typedef struct blaze_batch_hsp {

@@ -101,7 +101,8 @@ int main(void) {
                    (void *)blaze_batch_create, (void *)blaze_batch_free, (void *)blaze_batch_info,
                    (void *)blaze_search_run_batch, (void *)blaze_search_batch_results,
                    (void *)blaze_search_set_tuning, (void *)blaze_search_traceback,
-                   (void *)blaze_search_traceback_results, (void *)blaze_server_create,
+                   (void *)blaze_search_traceback_results, (void *)blaze_search_traceback_batch,
+                   (void *)blaze_search_traceback_batch_results, (void *)blaze_server_create,
                    (void *)blaze_server_submit, (void *)blaze_server_wait, (void *)blaze_server_take,
                    (void *)blaze_server_stats_get, (void *)blaze_server_free, (void *)blaze_volume_info,
                    (void *)blaze_volume_read, (void *)blaze_db_open, (void *)blaze_gapped_noalloc,

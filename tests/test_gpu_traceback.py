@@ -113,3 +113,34 @@ def test_traceback_to_tabular():
     assert ps.stats()["traceback_ms"] > 0
     ps.close()
     db.close()
+
+
+def test_traceback_batch_equals_single():
+    rng = np.random.default_rng(21)
+    qs = [synth.random_residues(rng, L) for L in (80, 300, 700, 1500)]
+    seqs = [synth.random_residues(rng, int(L)) for L in synth.lognormal_lengths(rng, 900, 250, 0.82, 30, 3000)]
+    for i in range(0, len(seqs), 4):
+        q = qs[i % len(qs)]
+        w = min(len(q), int(rng.integers(40, 300)))
+        s0 = int(rng.integers(0, len(q) - w + 1))
+        seqs[i] = np.concatenate([seqs[i], synth.mutate(rng, q[s0:s0 + w], 0.45)])
+    res, off = concat(seqs)
+    db = blaze103.SeqSrc(res, off)
+    ps = blaze103.PrelimSearch(db)
+    params = [blaze103.default_params(len(q), db) for q in qs]
+    singles = []
+    for q, p in zip(qs, params):
+        ps.run(q, p)
+        singles.append(ps.traceback(q, p))
+    batch = blaze103.QueryBatch(db, qs)
+    ps.run_batch(batch, params)
+    got = ps.traceback_batch(batch, params)
+    for i, want in enumerate(singles):
+        g = got[got["query"] == i]
+        for f in TB_FIELDS + ["oid"]:
+            assert np.array_equal(g[f], want[f]), (i, f)
+        assert np.allclose(g["evalue"], want["evalue"], rtol=1e-12)
+    assert len(got) == sum(len(w) for w in singles) > 20
+    batch.close()
+    ps.close()
+    db.close()
