@@ -10,16 +10,11 @@
 #include <numeric>
 #include <vector>
 
-#include "common.cuh"
+#include "handles.h"
 #include "internal.h"
-
-using namespace blaze;
 
 namespace {
 thread_local cudaError_t g_last_cuda = cudaSuccess;
-constexpr uint32_t kMaxSubjectLength = (1u << 28) - 64;  // diagonal table encoding limit
-constexpr int32_t kMaxQueryLength = 32000;                // diagonal table must fit shared memory
-constexpr uint32_t kInitialScratchCap = 1024;             // init hits per subject before a rerun
 }  // namespace
 
 void last_cuda_error(cudaError_t e) { g_last_cuda = e; }
@@ -27,128 +22,6 @@ int last_cuda_error_code() { return static_cast<int>(g_last_cuda); }
 void set_last_cuda_error_code(int code) { g_last_cuda = static_cast<cudaError_t>(code); }
 
 extern "C" const char *blaze_last_cuda_error(void) { return cudaGetErrorString(g_last_cuda); }
-
-struct blaze_db {
-    int device = 0;
-    uint8_t *d_res = nullptr;
-    uint64_t *d_off = nullptr;
-    uint64_t total = 0;
-    uint32_t n = 0;
-    uint32_t max_len = 0;
-    std::vector<uint32_t> oid_of;  // sorted index -> OID
-    std::vector<uint32_t> sorted_of;  // OID -> sorted index
-    std::vector<uint64_t> h_off;   // offsets of the length-sorted copy (host)
-};
-
-struct blaze_query {
-    int device = 0;
-    int32_t qlen = 0;
-    int32_t threshold = 0;
-    uint64_t upload_bytes = 0;  // host->device bytes of the tables
-    uint8_t *d_q = nullptr;
-    uint32_t *d_cell_start = nullptr;
-    uint32_t *d_cell_pack = nullptr;
-    uint32_t *d_presence = nullptr;
-    uint16_t *d_cell_off = nullptr;
-    uint32_t n_off = 0;
-};
-
-template <typename T>
-struct DevBuf {
-    T *p = nullptr;
-    size_t n = 0;
-    int ensure(size_t want) {
-        if (want <= n) return BLAZE_OK;
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-        BLAZE_CUDA_TRY(cudaMalloc(&p, sizeof(T) * std::max<size_t>(want, 1)));
-        n = want;
-        return BLAZE_OK;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-};
-
-struct blaze_search {
-    blaze_db *db = nullptr;
-    cudaStream_t stream = nullptr;
-    int n_sm = 0;
-    // per-run capacities
-    uint32_t scratch_cap = kInitialScratchCap;
-    unsigned long long init_cap = 0, out_cap = 0;
-    DevBuf<InitHit> scratch, init_out, sorted;
-    DevBuf<WorkItem> work;
-    DevBuf<DevHsp> saved, out;
-    DevBuf<int32_t> dp;
-    DevCounters *d_cnt = nullptr;
-    DevCounters *h_cnt = nullptr;  // pinned
-    DevHsp *h_out = nullptr;       // pinned
-    size_t h_out_n = 0;
-    int gapped_blocks = 0;
-    std::vector<blaze_hsp> results;
-    blaze_stats stats{};
-    unsigned long long last_init_count = 0, last_work_count = 0;
-    bool last_batched = false;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    // launch shape (blaze_search_set_tuning)
-    uint32_t stage_bytes = kScanStageBytes;
-    uint32_t tile_residues = 0;  // 0: automatic
-    // residue-balanced subject ranges of batched tiles, per tile size
-    std::map<uint32_t, DevBuf<uint32_t>> tile_bounds;
-    std::map<uint32_t, uint32_t> tile_ranges;
-    uint32_t max_warps = 0;
-    uint32_t launch_mode = 0;
-    // the per-pass launch sequence as a CUDA graph, and the arguments it was
-    // captured with
-    cudaGraphExec_t graph_exec = nullptr;
-    std::vector<unsigned char> graph_key;
-    // batched runs
-    unsigned long long work_cap = 0;
-    DevBuf<BatchQuery> bq;
-    DevBuf<const uint8_t *> bqptr;
-    DevBuf<int32_t> bqlen, bcut;
-    DevBuf<uint32_t> work_query, out_query;
-    DevBuf<unsigned long long> cursors;  // one work cursor per scan launch of a pass
-    uint32_t *h_outq = nullptr;  // pinned
-    size_t h_outq_n = 0;
-    std::vector<blaze_batch_hsp> batch_results;
-    // traceback stage
-    DevBuf<TbItem> tb_items;
-    DevBuf<TbOut> tb_out;
-    DevBuf<uint8_t> tb_dirs;
-    DevBuf<int32_t> tb_rows, tb_dp;
-    DevBuf<unsigned long long> tb_cursor;
-    unsigned long long tb_dir_cap = 1ull << 16;  // direction bytes per warp in a first pass
-    std::vector<blaze_aligned_hsp> tb_results;
-    std::vector<blaze_batch_aligned_hsp> tb_batch_results;
-    const blaze_batch *last_batch = nullptr;  // the batch of the last batched run
-};
-
-struct blaze_batch {
-    int device = 0;
-    uint32_t n = 0;
-    int32_t threshold = 0;
-    std::vector<int32_t> qlen;
-    std::vector<uint64_t> res_off, off_off;  // per query: residues, hit lists
-    // device tables; a refilled batch keeps them while they are large enough
-    DevBuf<uint8_t> res;
-    DevBuf<uint32_t> cell_start, cell_pack, presence;
-    DevBuf<uint16_t> cell_off;
-    uint8_t *d_res = nullptr;
-    uint32_t *d_cell_start = nullptr, *d_cell_pack = nullptr, *d_presence = nullptr;
-    uint16_t *d_cell_off = nullptr;
-    uint64_t upload_bytes = 0, device_bytes = 0;
-};
-
-static bool valid_residues(const uint8_t *r, uint64_t n) {
-    uint8_t bad = 0;
-    for (uint64_t i = 0; i < n; ++i) bad |= static_cast<uint8_t>(r[i] == 0) | static_cast<uint8_t>(r[i] >= kAlphabet);
-    return bad == 0;
-}
 
 extern "C" int blaze_device_count(int *count) {
     if (!count) return BLAZE_ERR_INVALID_ARG;
@@ -378,7 +251,7 @@ extern "C" int blaze_search_free(blaze_search *s) {
     return BLAZE_OK;
 }
 
-static int check_params(const blaze_params *p) {
+int check_params(const blaze_params *p) {
     if (!p) return BLAZE_ERR_INVALID_ARG;
     if (p->window <= 0 || p->window > (1 << 20) || p->ungapped_xdrop <= 0 || p->gap_open < 0 ||
         p->gap_extend <= 0 || p->gapped_xdrop <= 0 || p->gapped_cutoff <= 0 || p->ungapped_cutoff <= 0)
@@ -1000,145 +873,6 @@ extern "C" int blaze_search_stats(const blaze_search *s, blaze_stats *out) {
     return BLAZE_OK;
 }
 
-static int check_batch_input(const uint8_t *residues, const uint64_t *offsets, uint32_t n_queries) {
-    if (!residues || !offsets || n_queries == 0) return BLAZE_ERR_INVALID_ARG;
-    for (uint32_t i = 0; i < n_queries; ++i) {
-        if (offsets[i + 1] <= offsets[i]) return BLAZE_ERR_INVALID_ARG;
-        if (offsets[i + 1] - offsets[i] > static_cast<uint64_t>(kMaxQueryLength)) return BLAZE_ERR_LIMIT;
-        if (!valid_residues(residues + offsets[i], offsets[i + 1] - offsets[i])) return BLAZE_ERR_INVALID_ARG;
-    }
-    return BLAZE_OK;
-}
-
-// Builds the word tables of every query on the host and uploads them into
-// the batch's device buffers, growing those only when they are too small
-// (so that a refilled batch allocates nothing once it has seen its largest
-// load). Copies go on `stream` (0: synchronous).
-static int batch_fill(blaze_batch *b, const uint8_t *residues, const uint64_t *offsets, uint32_t n_queries,
-                      int32_t word_threshold, cudaStream_t stream) {
-    b->n = n_queries;
-    b->threshold = word_threshold;
-    b->qlen.clear();
-    b->res_off.clear();
-    b->off_off.clear();
-    std::vector<uint8_t> res;
-    std::vector<uint32_t> cs_all(static_cast<size_t>(n_queries) * (kWords + 1));
-    std::vector<uint32_t> pack_all(static_cast<size_t>(n_queries) * kWords);
-    std::vector<uint32_t> pres_all(static_cast<size_t>(n_queries) * kPresenceWords, 0u);
-    std::vector<uint16_t> offs_all;
-    for (uint32_t i = 0; i < n_queries; ++i) {
-        const int32_t len = static_cast<int32_t>(offsets[i + 1] - offsets[i]);
-        const uint8_t *q = residues + offsets[i];
-        b->qlen.push_back(len);
-        b->res_off.push_back(res.size());
-        res.insert(res.end(), q, q + len);
-        res.resize((res.size() + 63) & ~static_cast<size_t>(63), 0);  // 64-byte separation
-        uint32_t *cs = cs_all.data() + static_cast<size_t>(i) * (kWords + 1);
-        uint16_t *offs = nullptr;
-        uint32_t n_off = 0;
-        int rc = build_lookup(q, len, word_threshold, cs, &offs, &n_off);
-        if (rc != BLAZE_OK) return rc;
-        b->off_off.push_back(offs_all.size());
-        offs_all.insert(offs_all.end(), offs, offs + n_off);
-        std::free(offs);
-        uint32_t *pk = pack_all.data() + static_cast<size_t>(i) * kWords;
-        uint32_t *pr = pres_all.data() + static_cast<size_t>(i) * kPresenceWords;
-        for (int w = 0; w < kWords; ++w) {
-            const uint32_t cnt = cs[w + 1] - cs[w];
-            pk[w] = (cs[w] << 8) | std::min<uint32_t>(cnt, 255u);
-            if (cnt) pr[w >> 5] |= 1u << (w & 31);
-        }
-    }
-    res.resize(res.size() + 64, 0);
-    if (offs_all.empty()) offs_all.push_back(0);
-    // a refill grows by half again so that slowly rising loads settle
-    const size_t slack = stream ? 2 : 1;
-    auto grow = [&](auto &buf, size_t want) {
-        return want <= buf.n ? BLAZE_OK : buf.ensure(want + (slack - 1) * want / 2);
-    };
-    int rc = grow(b->res, res.size());
-    if (rc == BLAZE_OK) rc = grow(b->cell_start, cs_all.size());
-    if (rc == BLAZE_OK) rc = grow(b->cell_pack, pack_all.size());
-    if (rc == BLAZE_OK) rc = grow(b->presence, pres_all.size());
-    if (rc == BLAZE_OK) rc = grow(b->cell_off, offs_all.size());
-    if (rc != BLAZE_OK) return rc;
-    b->d_res = b->res.p;
-    b->d_cell_start = b->cell_start.p;
-    b->d_cell_pack = b->cell_pack.p;
-    b->d_presence = b->presence.p;
-    b->d_cell_off = b->cell_off.p;
-    auto put = [&](void *dst, const void *src, size_t bytes) {
-        return stream ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream)
-                      : cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
-    };
-    cudaError_t e = put(b->d_res, res.data(), res.size());
-    if (e == cudaSuccess) e = put(b->d_cell_start, cs_all.data(), sizeof(uint32_t) * cs_all.size());
-    if (e == cudaSuccess) e = put(b->d_cell_pack, pack_all.data(), sizeof(uint32_t) * pack_all.size());
-    if (e == cudaSuccess) e = put(b->d_presence, pres_all.data(), sizeof(uint32_t) * pres_all.size());
-    if (e == cudaSuccess) e = put(b->d_cell_off, offs_all.data(), sizeof(uint16_t) * offs_all.size());
-    // the host arrays die with this frame: the copies must have read them
-    if (e == cudaSuccess && stream) e = cudaStreamSynchronize(stream);
-    b->upload_bytes = res.size() + sizeof(uint32_t) * (cs_all.size() + pack_all.size() + pres_all.size()) +
-                      sizeof(uint16_t) * offs_all.size();
-    b->device_bytes = b->res.n + sizeof(uint32_t) * (b->cell_start.n + b->cell_pack.n + b->presence.n) +
-                      sizeof(uint16_t) * b->cell_off.n;
-    if (e != cudaSuccess) {
-        last_cuda_error(e);
-        return e == cudaErrorMemoryAllocation ? BLAZE_ERR_OUT_OF_MEMORY : BLAZE_ERR_CUDA;
-    }
-    return BLAZE_OK;
-}
-
-extern "C" int blaze_batch_create(const blaze_db *db, const uint8_t *residues, const uint64_t *offsets,
-                                  uint32_t n_queries, int32_t word_threshold, blaze_batch **out) {
-    if (!db || !out) return BLAZE_ERR_INVALID_ARG;
-    *out = nullptr;
-    const int vrc = check_batch_input(residues, offsets, n_queries);
-    if (vrc != BLAZE_OK) return vrc;
-    BLAZE_CUDA_TRY(cudaSetDevice(db->device));
-    auto *b = new blaze_batch();
-    b->device = db->device;
-    const int rc = batch_fill(b, residues, offsets, n_queries, word_threshold, nullptr);
-    if (rc != BLAZE_OK) {
-        blaze_batch_free(b);
-        return rc;
-    }
-    *out = b;
-    return BLAZE_OK;
-}
-
-int batch_refill(blaze_search *s, blaze_batch **inout, const uint8_t *residues, const uint64_t *offsets,
-                 uint32_t n_queries, int32_t word_threshold) {
-    if (!s || !inout) return BLAZE_ERR_INVALID_ARG;
-    const int vrc = check_batch_input(residues, offsets, n_queries);
-    if (vrc != BLAZE_OK) return vrc;
-    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
-    if (!*inout) {
-        *inout = new blaze_batch();
-        (*inout)->device = s->db->device;
-    }
-    return batch_fill(*inout, residues, offsets, n_queries, word_threshold, s->stream);
-}
-
-extern "C" int blaze_batch_free(blaze_batch *b) {
-    if (!b) return BLAZE_OK;
-    cudaSetDevice(b->device);
-    b->res.release();
-    b->cell_start.release();
-    b->cell_pack.release();
-    b->presence.release();
-    b->cell_off.release();
-    delete b;
-    return BLAZE_OK;
-}
-
-extern "C" int blaze_batch_info(const blaze_batch *b, uint32_t *n_queries, uint64_t *device_bytes) {
-    if (!b) return BLAZE_ERR_INVALID_ARG;
-    if (n_queries) *n_queries = b->n;
-    if (device_bytes) *device_bytes = b->device_bytes;
-    return BLAZE_OK;
-}
-
 extern "C" int blaze_search_init_hits(blaze_search *s, blaze_init_hit *out, uint64_t capacity,
                                       uint64_t *n_hits) {
     if (!s || s->last_batched) return BLAZE_ERR_INVALID_ARG;  // single-query runs only
@@ -1190,248 +924,4 @@ extern "C" int blaze_prelim_search(blaze_search *s, const uint8_t *query, int32_
     blaze_query_free(q);
     if (rc != BLAZE_OK) return rc;
     return blaze_search_results(s, out, capacity, n_hsps);
-}
-
-// ------------------------------------------------------------------------
-// Traceback stage.
-
-// Traces `items` in passes: the first over all of them with many warps and
-// small direction buffers, the next ones over those whose alignment did not
-// fit, with fewer warps and buffers four times larger. `q`/`qlen` is the
-// query of a single-query run; `batch_q`/`batch_qlen` (device arrays) the
-// queries of a batched run, indexed by TbItem::query.
-static int traceback_passes(blaze_search *s, const std::vector<TbItem> &items, const blaze_params *p,
-                            int32_t final_xdrop, const uint8_t *q, int32_t qlen, const uint8_t *const *batch_q,
-                            const int32_t *batch_qlen, int32_t max_qlen, std::vector<TbOut> &outs) {
-    const blaze_db *db = s->db;
-    const size_t n = items.size();
-    outs.assign(n, TbOut{});
-    s->stats.traceback_ms = 0.f;
-    s->stats.traceback_hsps = static_cast<uint32_t>(n);
-    s->stats.traceback_cells = 0;
-    std::vector<uint32_t> todo(n);
-    for (size_t i = 0; i < n; ++i) todo[i] = static_cast<uint32_t>(i);
-    unsigned long long cap = s->tb_dir_cap;
-    const uint32_t row_cap = static_cast<uint32_t>(max_qlen) + 2u;
-    const uint32_t dp_stride = std::max<uint32_t>(db->max_len, 1u) + 2u;
-    std::vector<TbItem> pass_items;
-    std::vector<TbOut> pass_out;
-    int rc;
-    for (int attempt = 0; !todo.empty(); ++attempt) {
-        if (attempt > 12) return BLAZE_ERR_LIMIT;
-        const size_t m = todo.size();
-        const int blocks = static_cast<int>(std::min<size_t>(static_cast<size_t>(s->n_sm) * 4,
-                                                             (m + kTracebackWarpsPerBlock - 1) / kTracebackWarpsPerBlock));
-        const size_t warps = static_cast<size_t>(blocks) * kTracebackWarpsPerBlock;
-        pass_items.resize(m);
-        for (size_t k = 0; k < m; ++k) pass_items[k] = items[todo[k]];
-        pass_out.resize(m);
-        if ((rc = s->tb_items.ensure(m)) != BLAZE_OK) return rc;
-        if ((rc = s->tb_out.ensure(m)) != BLAZE_OK) return rc;
-        if ((rc = s->tb_rows.ensure(warps * 3 * row_cap)) != BLAZE_OK) return rc;
-        if ((rc = s->tb_dp.ensure(warps * 2 * dp_stride)) != BLAZE_OK) return rc;
-        if ((rc = s->tb_cursor.ensure(1)) != BLAZE_OK) return rc;
-        if ((rc = s->tb_dirs.ensure(warps * cap)) != BLAZE_OK) return rc;
-        BLAZE_CUDA_TRY(cudaMemcpyAsync(s->tb_items.p, pass_items.data(), sizeof(TbItem) * m, cudaMemcpyHostToDevice,
-                                       s->stream));
-        s->stats.h2d_bytes += sizeof(TbItem) * m;
-        TracebackArgs ta{};
-        ta.res = db->d_res;
-        ta.off = db->d_off;
-        ta.q = q;
-        ta.qlen = qlen;
-        ta.batch_q = batch_q;
-        ta.batch_qlen = batch_qlen;
-        ta.items = s->tb_items.p;
-        ta.n_items = static_cast<uint32_t>(m);
-        ta.out = s->tb_out.p;
-        ta.gap_open = p->gap_open;
-        ta.gap_extend = p->gap_extend;
-        ta.xdrop = final_xdrop;
-        ta.dp = s->tb_dp.p;
-        ta.dp_stride = dp_stride;
-        ta.dirs = s->tb_dirs.p;
-        ta.dir_cap = cap;
-        ta.rows = s->tb_rows.p;
-        ta.row_cap = row_cap;
-        ta.cursor = s->tb_cursor.p;
-        BLAZE_CUDA_TRY(cudaMemsetAsync(s->tb_cursor.p, 0, sizeof(unsigned long long), s->stream));
-        BLAZE_CUDA_TRY(cudaEventRecord(s->ev[1], s->stream));
-        BLAZE_CUDA_TRY(launch_traceback(ta, blocks, s->stream));
-        BLAZE_CUDA_TRY(cudaEventRecord(s->ev[2], s->stream));
-        s->stats.kernel_launches += 1;
-        BLAZE_CUDA_TRY(cudaMemcpyAsync(pass_out.data(), s->tb_out.p, sizeof(TbOut) * m, cudaMemcpyDeviceToHost,
-                                       s->stream));
-        BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
-        s->stats.d2h_bytes += sizeof(TbOut) * m;
-        float ms = 0.f;
-        BLAZE_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev[1], s->ev[2]));
-        s->stats.traceback_ms += ms;
-        std::vector<uint32_t> again;
-        for (size_t k = 0; k < m; ++k) {
-            const TbOut &o = pass_out[k];
-            s->stats.traceback_cells += static_cast<uint64_t>(o.cells);
-            if (o.status == 2) return BLAZE_ERR_INTERNAL;
-            if (o.status == 1) again.push_back(todo[k]);
-            else outs[todo[k]] = o;
-        }
-        todo.swap(again);
-        cap *= 4;
-    }
-    return BLAZE_OK;
-}
-
-// One subject's traced HSPs: purged of shared start and end points (the
-// better kept), ordered as the preliminary stage orders them, given final
-// E-values and bit scores and reaped at `evalue`; appended to `out`.
-static void traceback_finish_subject(std::vector<TbOut> g, uint32_t oid, const blaze_params &p, double evalue,
-                                     std::vector<blaze_aligned_hsp> &out) {
-    auto by_start = [](const TbOut &a, const TbOut &b) {
-        if (a.q_start != b.q_start) return a.q_start < b.q_start;
-        if (a.s_start != b.s_start) return a.s_start < b.s_start;
-        if (a.score != b.score) return a.score > b.score;
-        if (a.q_end != b.q_end) return a.q_end > b.q_end;
-        return a.s_end > b.s_end;
-    };
-    auto by_end = [](const TbOut &a, const TbOut &b) {
-        if (a.q_end != b.q_end) return a.q_end < b.q_end;
-        if (a.s_end != b.s_end) return a.s_end < b.s_end;
-        if (a.score != b.score) return a.score > b.score;
-        if (a.q_start != b.q_start) return a.q_start < b.q_start;
-        return a.s_start < b.s_start;
-    };
-    auto by_score = [](const TbOut &a, const TbOut &b) {
-        if (a.score != b.score) return a.score > b.score;
-        if (a.s_start != b.s_start) return a.s_start < b.s_start;
-        if (a.s_end != b.s_end) return a.s_end > b.s_end;
-        if (a.q_start != b.q_start) return a.q_start < b.q_start;
-        return a.q_end > b.q_end;
-    };
-    std::stable_sort(g.begin(), g.end(), by_start);
-    std::vector<TbOut> m;
-    for (const TbOut &o : g)
-        if (m.empty() || o.q_start != m.back().q_start || o.s_start != m.back().s_start) m.push_back(o);
-    std::stable_sort(m.begin(), m.end(), by_end);
-    std::vector<TbOut> m2;
-    for (const TbOut &o : m)
-        if (m2.empty() || o.q_end != m2.back().q_end || o.s_end != m2.back().s_end) m2.push_back(o);
-    std::stable_sort(m2.begin(), m2.end(), by_score);
-    const double ln2 = std::log(2.0), lnK = std::log(p.K);
-    for (const TbOut &o : m2) {
-        blaze_aligned_hsp h{};
-        h.oid = oid;
-        h.score = o.score;
-        h.q_start = o.q_start;
-        h.q_end = o.q_end;
-        h.s_start = o.s_start;
-        h.s_end = o.s_end;
-        h.length = o.length;
-        h.identities = o.identities;
-        h.positives = o.positives;
-        h.mismatches = o.mismatches;
-        h.gap_opens = o.gap_opens;
-        h.gaps = o.gaps;
-        h.evalue = p.eff_searchsp * p.K * std::exp(-p.lambda * static_cast<double>(o.score));
-        h.bit_score = (p.lambda * static_cast<double>(o.score) - lnK) / ln2;
-        if (h.evalue <= evalue) out.push_back(h);
-    }
-}
-
-static int tb_item(const blaze_db *db, const blaze_hsp &h, int32_t qlen, uint32_t query, TbItem *it) {
-    if (h.oid >= db->n || h.q_gapped_start < 0 || h.q_gapped_start >= qlen) return BLAZE_ERR_INVALID_ARG;
-    const uint32_t sub = db->sorted_of[h.oid];
-    if (h.s_gapped_start < 0 || static_cast<uint64_t>(h.s_gapped_start) >= db->h_off[sub + 1] - db->h_off[sub])
-        return BLAZE_ERR_INVALID_ARG;
-    *it = TbItem{sub, h.q_gapped_start, h.s_gapped_start, query};
-    return BLAZE_OK;
-}
-
-extern "C" int blaze_search_traceback(blaze_search *s, const blaze_query *q, const blaze_params *p,
-                                      int32_t final_xdrop, double evalue, uint64_t *n_hsps) {
-    if (!s || !q || !p || final_xdrop <= 0 || q->device != s->db->device || s->last_batched)
-        return BLAZE_ERR_INVALID_ARG;
-    int rc = check_params(p);
-    if (rc != BLAZE_OK) return rc;
-    if (n_hsps) *n_hsps = 0;
-    s->tb_results.clear();
-    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
-    const size_t n = s->results.size();
-    std::vector<TbItem> items(n);
-    for (size_t i = 0; i < n; ++i)
-        if ((rc = tb_item(s->db, s->results[i], q->qlen, 0u, &items[i])) != BLAZE_OK) return rc;
-    std::vector<TbOut> outs;
-    if ((rc = traceback_passes(s, items, p, final_xdrop, q->d_q, q->qlen, nullptr, nullptr, q->qlen, outs)) !=
-        BLAZE_OK)
-        return rc;
-    for (size_t i = 0; i < n;) {
-        size_t j = i;
-        while (j < n && s->results[j].oid == s->results[i].oid) ++j;
-        traceback_finish_subject(std::vector<TbOut>(outs.begin() + i, outs.begin() + j), s->results[i].oid, *p,
-                                 evalue, s->tb_results);
-        i = j;
-    }
-    if (n_hsps) *n_hsps = s->tb_results.size();
-    return BLAZE_OK;
-}
-
-extern "C" int blaze_search_traceback_batch(blaze_search *s, const blaze_batch *b, const blaze_params *params,
-                                            int32_t final_xdrop, double evalue, uint64_t *n_hsps) {
-    if (!s || !b || !params || final_xdrop <= 0 || !s->last_batched || s->last_batch != b)
-        return BLAZE_ERR_INVALID_ARG;
-    int rc;
-    for (uint32_t i = 0; i < b->n; ++i)
-        if ((rc = check_params(&params[i])) != BLAZE_OK) return rc;
-    if (n_hsps) *n_hsps = 0;
-    s->tb_batch_results.clear();
-    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
-    const size_t n = s->batch_results.size();
-    std::vector<TbItem> items(n);
-    int32_t max_qlen = 1;
-    for (uint32_t i = 0; i < b->n; ++i) max_qlen = std::max(max_qlen, b->qlen[i]);
-    for (size_t i = 0; i < n; ++i) {
-        const blaze_batch_hsp &bh = s->batch_results[i];
-        if (bh.query >= b->n) return BLAZE_ERR_INVALID_ARG;
-        if ((rc = tb_item(s->db, bh.hsp, b->qlen[bh.query], bh.query, &items[i])) != BLAZE_OK) return rc;
-    }
-    // the per-query arrays of the last batched run (batch order) are still
-    // on the device
-    std::vector<TbOut> outs;
-    if ((rc = traceback_passes(s, items, &params[0], final_xdrop, nullptr, 0, s->bqptr.p, s->bqlen.p, max_qlen,
-                               outs)) != BLAZE_OK)
-        return rc;
-    std::vector<blaze_aligned_hsp> one;
-    for (size_t i = 0; i < n;) {
-        size_t j = i;
-        const uint32_t qi = s->batch_results[i].query, oid = s->batch_results[i].hsp.oid;
-        while (j < n && s->batch_results[j].query == qi && s->batch_results[j].hsp.oid == oid) ++j;
-        one.clear();
-        traceback_finish_subject(std::vector<TbOut>(outs.begin() + i, outs.begin() + j), oid, params[qi], evalue,
-                                 one);
-        for (const blaze_aligned_hsp &h : one) s->tb_batch_results.push_back(blaze_batch_aligned_hsp{qi, 0u, h});
-        i = j;
-    }
-    if (n_hsps) *n_hsps = s->tb_batch_results.size();
-    return BLAZE_OK;
-}
-
-extern "C" int blaze_search_traceback_batch_results(const blaze_search *s, blaze_batch_aligned_hsp *out,
-                                                    uint64_t capacity, uint64_t *n_hsps) {
-    if (!s) return BLAZE_ERR_INVALID_ARG;
-    const size_t n = s->tb_batch_results.size();
-    if (n_hsps) *n_hsps = n;
-    if (capacity < n) return BLAZE_ERR_OUTPUT_TOO_SMALL;
-    if (n && !out) return BLAZE_ERR_INVALID_ARG;
-    if (n) std::memcpy(out, s->tb_batch_results.data(), sizeof(blaze_batch_aligned_hsp) * n);
-    return BLAZE_OK;
-}
-
-extern "C" int blaze_search_traceback_results(const blaze_search *s, blaze_aligned_hsp *out, uint64_t capacity,
-                                              uint64_t *n_hsps) {
-    if (!s) return BLAZE_ERR_INVALID_ARG;
-    const size_t n = s->tb_results.size();
-    if (n_hsps) *n_hsps = n;
-    if (capacity < n) return BLAZE_ERR_OUTPUT_TOO_SMALL;
-    if (n && !out) return BLAZE_ERR_INVALID_ARG;
-    if (n) std::memcpy(out, s->tb_results.data(), sizeof(blaze_aligned_hsp) * n);
-    return BLAZE_OK;
 }
