@@ -209,3 +209,21 @@ def test_sharded_search_one_rank_matches_plain(tmp_path):
             assert np.array_equal(got[f], want[f]), f
     ps.close()
     db.close()
+
+
+def test_homopolymer_query_and_degenerate_databases():
+    # a word with more than 255 query positions takes the overflow path of the
+    # packed cells; runs in the subjects flood the seed and deferral queues
+    rng = np.random.default_rng(255)
+    q = np.full(600, 11, dtype=np.uint8)  # L x 600
+    seqs = [synth.random_residues(rng, int(rng.integers(50, 900))) for _ in range(60)]
+    for i in range(0, 60, 3):
+        seqs[i] = np.concatenate([seqs[i], np.full(int(rng.integers(20, 300)), 11, dtype=np.uint8)])
+    res, off = concat(seqs)
+    got, _, stats = compare(q, res, off)
+    assert len(got) > 0 and stats["ungapped_extensions"] > 100
+    # databases with no word at all: empty, and only subjects shorter than a word
+    for seqs in ([], [q[:0], q[:1], q[:2]]):
+        res, off = concat(seqs) if seqs else (np.zeros(0, np.uint8), np.zeros(1, np.uint64))
+        got, ref, _ = compare(synth.random_residues(rng, 50), res, off)
+        assert len(got) == 0 and len(ref) == 0
