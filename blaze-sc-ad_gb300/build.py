@@ -33,11 +33,9 @@ def _compile(src: str, verbose: bool) -> tuple[str, str]:
     obj = os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
            "-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj]
-    if src.endswith(".cu"):
-        cmd[1:1] = ["-Xptxas", "-v"] if verbose else []
-    else:
-        cmd += ["-x", "cu"] if False else []
-    r = subprocess.run(cmd, capture_output=True, text=True)
+    if src.endswith(".cu") and verbose:
+        cmd[1:1] = ["-Xptxas", "-v"]
+    r =subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
     return obj, r.stderr
