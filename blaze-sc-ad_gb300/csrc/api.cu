@@ -465,7 +465,10 @@ static int run_pass(blaze_search *s, const RunSpec &r, const std::vector<ScanPla
         if (batched) {
             sa.queries = s->bq.p + plan.first;
             sa.n_queries = plan.n;
-            if ((rc = tile_bounds_for(s, plan.tile_residues, &sa.tile_bounds, &sa.n_ranges)) != BLAZE_OK) return rc;
+            // a tile is one block's work: tile_residues per warp
+            const uint32_t block_tile = static_cast<uint32_t>(std::min<uint64_t>(
+                static_cast<uint64_t>(plan.tile_residues) * static_cast<uint64_t>(lay.warps_per_block), 1u << 31));
+            if ((rc = tile_bounds_for(s, block_tile, &sa.tile_bounds, &sa.n_ranges)) != BLAZE_OK) return rc;
             sa.work_query = s->work_query.p;
         } else {
             const blaze_query *q = r.q;
@@ -544,22 +547,13 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
     if (n_hsps) *n_hsps = 0;
 
     constexpr size_t kSmemBudget = 220 * 1024;
-    const int reg_cap = batched ? scan_batch_max_warps_by_registers()
+    const int reg_cap = batched ? std::min(scan_batch_max_warps_by_registers(true),
+                                           scan_batch_max_warps_by_registers(false))
                                 : scan_max_warps_by_registers(r.q->qlen <= static_cast<int32_t>(kQuerySmemMax));
     const int warp_cap = s->max_warps ? std::min(reg_cap, static_cast<int>(s->max_warps)) : reg_cap;
     // layout of one scan launch for queries up to max_qlen
     auto layout_for = [&](int32_t max_qlen) {
-        ScanLayout lay = scan_layout(max_qlen, p0->window, s->stage_bytes, kSmemBudget, warp_cap);
-        if (batched) {
-            // the batched kernel keeps every query in global memory
-            const size_t fixed = kScanMatBytes + kScanPresenceBytes;
-            lay.query_smem_bytes = 0;
-            int w = lay.warps_per_block;
-            while (w < warp_cap && fixed + static_cast<size_t>(w + 1) * lay.warp_smem_bytes <= kSmemBudget) ++w;
-            lay.warps_per_block = w;
-            lay.smem_bytes = fixed + static_cast<size_t>(w) * lay.warp_smem_bytes;
-        }
-        return lay;
+        return scan_layout(max_qlen, p0->window, s->stage_bytes, kSmemBudget, warp_cap);
     };
     // Length classes: a launch sizes every warp's diagonal table for its
     // longest query, so a batch is split, shortest first, into classes whose
@@ -583,7 +577,8 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
         if (pl.lay.smem_bytes > 227 * 1024) return BLAZE_ERR_LIMIT;
         int per_sm = 0;
         if (batched) {
-            BLAZE_CUDA_TRY(scan_batch_occupancy(pl.lay.warps_per_block, pl.lay.smem_bytes, &per_sm));
+            BLAZE_CUDA_TRY(scan_batch_occupancy(pl.lay.query_smem_bytes != 0, pl.lay.warps_per_block, pl.lay.smem_bytes,
+                                                &per_sm));
         } else {
             BLAZE_CUDA_TRY(scan_occupancy(pl.lay.query_smem_bytes != 0, pl.lay.warps_per_block, pl.lay.smem_bytes, &per_sm));
         }
@@ -593,8 +588,9 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
             if (s->tile_residues) {
                 pl.tile_residues = s->tile_residues;
             } else {
-                // several tiles per warp, at most kMaxTileResidues each; a
-                // power of two so that few distinct bound tables exist
+                // several tiles' worth per warp, at most kMaxTileResidues
+                // each (a block's tile is that times its warps); a power of
+                // two so that few distinct bound tables exist
                 const uint64_t warps = static_cast<uint64_t>(pl.blocks) * pl.lay.warps_per_block;
                 const uint64_t ranges = (4 * warps + pl.n - 1) / pl.n;
                 uint64_t t = std::max<uint64_t>(db->total / std::max<uint64_t>(ranges, 1), 1);

@@ -188,8 +188,8 @@ cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st);
 constexpr int kTracebackWarpsPerBlock = 4;
 cudaError_t launch_traceback(const TracebackArgs &a, int n_blocks, cudaStream_t st);
 cudaError_t launch_scan_batch(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem, cudaStream_t st);
-cudaError_t scan_batch_occupancy(int warps_per_block, size_t smem, int *blocks_per_sm);
-int scan_batch_max_warps_by_registers();
+cudaError_t scan_batch_occupancy(bool query_in_smem, int warps_per_block, size_t smem, int *blocks_per_sm);
+int scan_batch_max_warps_by_registers(bool query_in_smem);
 cudaError_t gapped_occupancy(int *blocks_per_sm);
 
 // Host helpers (host.cpp).

@@ -706,30 +706,43 @@ scan_kernel(const ScanArgs a) {
     finish_counters(a, f, word_hits, residues);
 }
 
-// Many queries against the database: warps pull (query, subject range)
+// Many queries against the database: blocks pull (query, subject range)
 // tiles; tile t covers query t mod n_queries and the (t / n_queries)-th
 // range counted from the longest subjects down, so every query's long
 // subjects come first and queries interleave. Ranges hold about equal
-// residues (host-computed bounds), so no tile holds up the end of the
-// launch. Query tables stay in global memory (L1/L2 resident).
+// residues (host-computed bounds, sized for a whole block). A block stages
+// its tile's query tables in shared memory -- the word-presence bitset and,
+// up to kQuerySmemMax residues, the query -- and its warps take the range's
+// subjects longest first from a shared cursor; the block restages only
+// after every warp has left the tile.
+template <bool QS>
 __global__ void __launch_bounds__(kScanMaxWarpsPerBlock * 32, 1)
 scan_batch_kernel(const ScanArgs a) {
+    __shared__ unsigned long long s_tile;
+    __shared__ uint32_t s_next;
     const int lane = threadIdx.x & 31;
     for (int i = threadIdx.x; i < kAlphabet * kAlphabet; i += blockDim.x)
         reinterpret_cast<int8_t *>(smem)[kMatOff + i] = g_blosum8[i];
     uint32_t stage = 0;
-    Finder f = make_finder(a, 0u, stage);
-    __syncthreads();
+    Finder f = make_finder(a, a.query_smem_bytes, stage);
     const unsigned long long n_tiles = static_cast<unsigned long long>(a.n_ranges) * a.n_queries;
     unsigned long long word_hits = 0, residues = 0;
+    bool staging = true;  // false after a bulk copy that never landed (kFlagBadState is set)
     for (;;) {
-        unsigned long long t = 0;
-        if (lane == 0) t = atomicAdd(a.cursor, 1ull);
-        t = __shfl_sync(kFull, t, 0);
+        if (threadIdx.x == 0) {
+            s_tile = atomicAdd(a.cursor, 1ull);
+            s_next = 0u;
+        }
+        __syncthreads();  // also orders the previous tile's last table reads before the restage
+        const unsigned long long t = s_tile;
         if (t >= n_tiles) break;
         const uint32_t qi = static_cast<uint32_t>(t % a.n_queries);
         const uint32_t range = static_cast<uint32_t>(t / a.n_queries);
         const BatchQuery bq = a.queries[qi];
+        for (int i = threadIdx.x; i < kPresenceWords; i += blockDim.x) sts32(kPresOff + 4u * i, bq.presence[i]);
+        if (QS)
+            for (int i = threadIdx.x; i < bq.qlen; i += blockDim.x) smem[kQueryOff + i] = bq.q[i];
+        __syncthreads();
         Ctx c;
         c.q = bq.q;
         c.qlen = bq.qlen;
@@ -742,16 +755,27 @@ scan_batch_kernel(const ScanArgs a) {
         c.window = a.window;
         c.xdrop = a.xdrop;
         c.cutoff = bq.ungapped_cutoff;
-        Query<false> q;
+        Query<QS> q;
         q.ptr = bq.q;
         q.len = bq.qlen;
         const uint32_t hi = a.tile_bounds[range], lo = a.tile_bounds[range + 1];
-        for (uint32_t subj = hi; subj-- > lo;) {
-            const bool staged = stage_issue(f, a, stage, 0, subj);
-            if (staged && !stage_wait(f, a, 0)) return;
-            process_subject<false, false>(f, a, c, q, subj, bq.index, staged ? stage : kNoStage, word_hits,
-                                          residues);
+        for (;;) {
+            uint32_t k = 0;
+            if (lane == 0) k = atomicAdd(&s_next, 1u);
+            k = __shfl_sync(kFull, k, 0);
+            if (k >= hi - lo) break;
+            const uint32_t subj = hi - 1u - k;
+            bool staged = staging && stage_issue(f, a, stage, 0, subj);
+            if (staged && !stage_wait(f, a, 0)) {
+                // the copy never landed: read this and every later subject
+                // from global memory (the host reports the run as failed)
+                staging = false;
+                staged = false;
+            }
+            process_subject<QS, true>(f, a, c, q, subj, bq.index, staged ? stage : kNoStage, word_hits,
+                                      residues);
         }
+        __syncthreads();
     }
     finish_counters(a, f, word_hits, residues);
 }
@@ -788,8 +812,14 @@ static cudaError_t allow_full_smem(const void *kernel) {
     std::lock_guard<std::mutex> lk(mu);
     if (done.count({dev, kernel})) return cudaSuccess;
     int optin = 0;
+    cudaFuncAttributes fa{};
     e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    // the dynamic allowance plus the kernel's static shared memory may not
+    // exceed the opt-in limit
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kernel);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 optin - static_cast<int>(fa.sharedSizeBytes));
     if (e == cudaSuccess) done.insert({dev, kernel});
     return e;
 }
@@ -814,24 +844,29 @@ int scan_max_warps_by_registers(bool query_in_smem) {
     return per_warp > 0 ? std::max(1, std::min(kScanMaxWarpsPerBlock, std::min(fa.maxThreadsPerBlock / 32, regs_per_block / per_warp))) : kScanMaxWarpsPerBlock;
 }
 
+static void (*batch_kernel(bool query_in_smem))(ScanArgs) {
+    return query_in_smem ? scan_batch_kernel<true> : scan_batch_kernel<false>;
+}
+
 cudaError_t launch_scan_batch(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem_bytes,
                               cudaStream_t st) {
-    cudaError_t e = allow_full_smem(reinterpret_cast<const void *>(scan_batch_kernel));
+    auto kernel = batch_kernel(a.query_smem_bytes != 0);
+    cudaError_t e = allow_full_smem(reinterpret_cast<const void *>(kernel));
     if (e != cudaSuccess) return e;
-    scan_batch_kernel<<<n_blocks, warps_per_block * 32, smem_bytes, st>>>(a);
+    kernel<<<n_blocks, warps_per_block * 32, smem_bytes, st>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t scan_batch_occupancy(int warps_per_block, size_t smem_bytes, int *blocks_per_sm) {
-    cudaError_t e = allow_full_smem(reinterpret_cast<const void *>(scan_batch_kernel));
+cudaError_t scan_batch_occupancy(bool query_in_smem, int warps_per_block, size_t smem_bytes, int *blocks_per_sm) {
+    auto kernel = batch_kernel(query_in_smem);
+    cudaError_t e = allow_full_smem(reinterpret_cast<const void *>(kernel));
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, scan_batch_kernel, warps_per_block * 32,
-                                                         smem_bytes);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel, warps_per_block * 32, smem_bytes);
 }
 
-int scan_batch_max_warps_by_registers() {
+int scan_batch_max_warps_by_registers(bool query_in_smem) {
     cudaFuncAttributes fa{};
-    if (cudaFuncGetAttributes(&fa, scan_batch_kernel) != cudaSuccess) return kScanMaxWarpsPerBlock;
+    if (cudaFuncGetAttributes(&fa, batch_kernel(query_in_smem)) != cudaSuccess) return kScanMaxWarpsPerBlock;
     int dev = 0, regs_per_block = 65536;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&regs_per_block, cudaDevAttrMaxRegistersPerBlock, dev);

@@ -253,10 +253,11 @@ int blaze_search_batch_results(const blaze_search *s, blaze_batch_hsp *out, uint
                                uint64_t *n_hsps);
 
 /* Launch shape of the word finder (0 = library default): subjects up to
- * stage_bytes residues are staged in shared memory; a batched tile covers
- * consecutive subjects of about tile_residues residues (a longer subject is
- * a tile of its own; 0: sized so that every warp gets several tiles);
- * max_warps_per_block caps the block. */
+ * stage_bytes residues are staged in shared memory; a batched tile is one
+ * block's work for one query: consecutive subjects of about tile_residues
+ * residues per warp of the block (a longer subject is a tile of its own; 0:
+ * sized so that every warp gets several tiles' worth); max_warps_per_block
+ * caps the block. */
 typedef struct blaze_tuning {
     uint32_t stage_bytes;
     uint32_t tile_residues;
