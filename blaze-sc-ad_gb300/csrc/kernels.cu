@@ -64,7 +64,10 @@ __device__ int32_t gapped_start(const uint8_t *q, const uint8_t *s, int32_t q_st
 // seen so far in row-major order. Cells below that bound can never become
 // live again, so computing the prefix maxima over every cell of the band
 // (live or not) leaves all live values and the live set exactly those of the
-// sequential band algorithm the oracle runs.
+// sequential band algorithm the oracle runs. The running best's prefix
+// maximum is taken only in a 32-column step whose largest value beats the
+// best carried into it (a warp max-reduce decides); in every other step the
+// carried best is each cell's best so far.
 template <bool REV>
 __device__ int32_t xdrop_dp(const uint8_t *__restrict__ A, const uint8_t *__restrict__ B, int32_t M,
                             int32_t N, int32_t gap_open, int32_t gap_extend, int32_t xdrop,
@@ -110,23 +113,27 @@ __device__ int32_t xdrop_dp(const uint8_t *__restrict__ A, const uint8_t *__rest
             excl = max(excl, carry_p);
             const int32_t G = excl - goe + ge - ge * b;
             const int32_t H = max(D, G);
-            int32_t inclh = act ? H : INT32_MIN;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int32_t x = __shfl_up_sync(kFull, inclh, o);
-                if (lane >= o) inclh = max(inclh, x);
-            }
-            int32_t exclh = __shfl_up_sync(kFull, inclh, 1);
-            if (lane == 0) exclh = INT32_MIN;
-            const int32_t cur_best = max(carry_best, exclh);
-            const bool alive = act && (cur_best - H <= xdrop);
-            const int32_t cm = __shfl_sync(kFull, inclh, 31);
+            // the best so far in row-major order: only a segment whose largest
+            // H beats the carried best needs the prefix maximum
+            const int32_t hv = act ? H : INT32_MIN;
+            const int32_t cm = __reduce_max_sync(kFull, hv);
+            int32_t cur_best = carry_best;
             if (cm > carry_best) {
+                int32_t inclh = hv;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int32_t x = __shfl_up_sync(kFull, inclh, o);
+                    if (lane >= o) inclh = max(inclh, x);
+                }
+                int32_t exclh = __shfl_up_sync(kFull, inclh, 1);
+                if (lane == 0) exclh = INT32_MIN;
+                cur_best = max(carry_best, exclh);
                 const unsigned mm = __ballot_sync(kFull, act && H == cm);
                 row_best = cm;
                 row_best_b = c0 + __ffs(mm) - 1;
                 carry_best = cm;
             }
+            const bool alive = act && (cur_best - H <= xdrop);
             const unsigned am = __ballot_sync(kFull, alive);
             if (am) {
                 if (first_alive < 0) first_alive = c0 + __ffs(am) - 1;

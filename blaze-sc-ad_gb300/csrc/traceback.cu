@@ -102,23 +102,27 @@ __device__ int32_t xdrop_dp_dirs(const uint8_t *__restrict__ A, const uint8_t *_
             excl = max(excl, carry_p);
             const int32_t G = excl - goe + ge - ge * b;
             const int32_t H = max(D, G);
-            int32_t inclh = act ? H : INT32_MIN;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int32_t x = __shfl_up_sync(kFull, inclh, o);
-                if (lane >= o) inclh = max(inclh, x);
-            }
-            int32_t exclh = __shfl_up_sync(kFull, inclh, 1);
-            if (lane == 0) exclh = INT32_MIN;
-            const int32_t cur_best = max(carry_best, exclh);
-            const bool alive = act && (cur_best - H <= xdrop);
-            const int32_t cm = __shfl_sync(kFull, inclh, 31);
+            // the best so far in row-major order: only a segment whose largest
+            // H beats the carried best needs the prefix maximum
+            const int32_t hv = act ? H : INT32_MIN;
+            const int32_t cm = __reduce_max_sync(kFull, hv);
+            int32_t cur_best = carry_best;
             if (cm > carry_best) {
+                int32_t inclh = hv;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int32_t x = __shfl_up_sync(kFull, inclh, o);
+                    if (lane >= o) inclh = max(inclh, x);
+                }
+                int32_t exclh = __shfl_up_sync(kFull, inclh, 1);
+                if (lane == 0) exclh = INT32_MIN;
+                cur_best = max(carry_best, exclh);
                 const unsigned mm = __ballot_sync(kFull, act && H == cm);
                 row_best = cm;
                 row_best_b = c0 + __ffs(mm) - 1;
                 carry_best = cm;
             }
+            const bool alive = act && (cur_best - H <= xdrop);
             const unsigned am = __ballot_sync(kFull, alive);
             if (am) {
                 if (first_alive < 0) first_alive = c0 + __ffs(am) - 1;
