@@ -37,7 +37,7 @@ SHAPES = {
 GRID = {
     "stage_bytes": (1024, 2048, 4096),
     "max_warps_per_block": (8, 16, 0),  # 0: as many as registers allow
-    "tile_residues": (0, 4096, 65536),  # 0: several tiles per warp
+    "tile_residues": (0, 4096, 65536),  # per warp of a block tile; 0: several tiles' worth per warp
 }
 
 _cache = None

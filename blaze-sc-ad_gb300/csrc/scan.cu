@@ -2,9 +2,10 @@
 // the BLASTP preliminary search on GB300 (sm_103a). Integer work only.
 //
 // One warp per subject; persistent warps pull subjects, longest first, from a
-// device cursor. Per block in shared memory: the BLOSUM62 matrix (int8), the
-// query's word-presence bitset and, for queries up to kQuerySmemMax, the
-// query residues. Per warp: the diagonal table, the deferred-hit and seed
+// device cursor (batched: blocks pull (query, subject range) tiles, their
+// warps the tile's subjects). Per block in shared memory: the BLOSUM62 matrix
+// (int8), the query's word-presence bitset and, for queries up to
+// kQuerySmemMax, the query residues. Per warp: the diagonal table, the deferred-hit and seed
 // queues and a staging buffer that holds the whole subject when it fits, so
 // the word scan and the extensions read shared memory instead of making
 // dependent global loads.
