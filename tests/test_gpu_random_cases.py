@@ -1,0 +1,135 @@
+"""Randomised parity cases on cuda:0: seeded random databases (empty,
+single-subject and long subjects, rare residue codes, low-complexity runs,
+planted homologs, unsorted OIDs), queries of 1 to 12,000 residues, varied
+search parameters and launch shapes. Each case checks the plain search
+against the oracle (init hits and HSPs), and some also the traceback against
+the oracle's and a batched run against the plain runs of its queries."""
+import numpy as np
+import pytest
+
+import blaze103
+import oracle
+from blaze103 import synth
+
+from _parity import compare, concat, params_for
+
+pytestmark = pytest.mark.gpu
+
+TB_FIELDS = ["score", "q_start", "q_end", "s_start", "s_end", "length", "identities", "mismatches", "gap_opens",
+             "gaps"]
+RARE = np.array([21, 24, 2, 23, 25, 26, 27, 22], dtype=np.uint8)  # X U B Z * O J Y
+
+
+def make_case(rng):
+    """One random case: (query, subjects, parameter overrides, launch shape)."""
+    r = rng.random()
+    if r < 0.08:
+        qlen = int(rng.integers(1, 12))
+    elif r < 0.85:
+        qlen = int(np.clip(rng.lognormal(np.log(300), 0.7), 12, 3000))
+    elif r < 0.95:
+        qlen = int(rng.integers(3000, 8200))
+    else:  # longer than the shared-memory copy of the query
+        qlen = int(rng.integers(8193, 12000))
+    q = synth.random_residues(rng, qlen)
+    n = int(rng.choice([1, 2, 7, 50, 300, 1500]))
+    med = float(rng.choice([15, 80, 250, 700]))
+    lens = np.clip(rng.lognormal(np.log(med), 0.9, n), 0, 6000).astype(int)
+    if rng.random() < 0.1:
+        lens[rng.integers(0, n)] = int(rng.integers(6000, 40000))
+    budget_res = 3_000_000 if qlen < 3000 else 600_000
+    while lens.sum() > budget_res and len(lens) > 1:
+        lens = lens[: len(lens) // 2]
+    seqs = [synth.random_residues(rng, int(L)) for L in lens]
+    for i in range(len(seqs)):
+        u = rng.random()
+        if u < 0.15 and qlen >= 20:  # homolog
+            w = min(qlen, int(rng.integers(15, 400)))
+            s0 = int(rng.integers(0, qlen - w + 1))
+            hom = synth.mutate(rng, q[s0:s0 + w], float(rng.uniform(0.3, 0.95)))
+            p = int(rng.integers(0, len(seqs[i]) + 1))
+            seqs[i] = np.concatenate([seqs[i][:p], hom, seqs[i][p:]])
+        elif u < 0.22:  # low complexity run
+            alpha = rng.choice(np.arange(1, 26, dtype=np.uint8), 3, replace=False)
+            run = alpha[rng.integers(0, 3, int(rng.integers(20, 300)))]
+            p = int(rng.integers(0, len(seqs[i]) + 1))
+            seqs[i] = np.concatenate([seqs[i][:p], run, seqs[i][p:]])
+        if rng.random() < 0.05 and len(seqs[i]):
+            k = int(rng.integers(1, 6))
+            idx = rng.integers(0, len(seqs[i]), k)
+            seqs[i] = seqs[i].copy()
+            seqs[i][idx] = RARE[rng.integers(0, len(RARE), k)]
+    if rng.random() < 0.05 and qlen:
+        q = q.copy()
+        q[rng.integers(0, qlen, 3)] = RARE[rng.integers(0, len(RARE), 3)]
+    if rng.random() < 0.3:  # unsorted OIDs
+        perm = rng.permutation(len(seqs))
+        seqs = [seqs[i] for i in perm]
+    override = {}
+    if rng.random() < 0.3:
+        override["window"] = int(rng.choice([20, 40, 60, 100]))
+    if rng.random() < 0.2:
+        override["word_threshold"] = int(rng.choice([10, 12, 13, 15]))
+    if rng.random() < 0.2:
+        go, ge = [(11, 1), (10, 2), (9, 1), (12, 3)][int(rng.integers(0, 4))]
+        override["gap_open"] = go
+        override["gap_extend"] = ge
+    if rng.random() < 0.2:
+        override["ungapped_xdrop"] = int(rng.choice([8, 12, 25, 40]))
+    if rng.random() < 0.2:
+        override["gapped_xdrop"] = int(rng.choice([15, 25, 60, 100]))
+    tuning = None
+    if rng.random() < 0.3:
+        tuning = dict(stage_bytes=int(rng.choice([0, 128, 256, 4096, 16384])),
+                      max_warps_per_block=int(rng.choice([0, 1, 4, 13, 32])))
+    return q, seqs, override, tuning
+
+
+
+def run_case(seed):
+    rng = np.random.default_rng(seed)
+    q, seqs, override, tuning = make_case(rng)
+    res, off = concat(seqs)
+    db = blaze103.SeqSrc(res, off, device=0)
+    ps = blaze103.PrelimSearch(db, autotune=False)
+    try:
+        if tuning:
+            ps.set_tuning(**tuning)
+        got, ref, _ = compare(q, res, off, seq_src=db, search=ps, **override)
+        if len(got) and rng.random() < 0.5 and not override.get("gap_extend"):
+            p, pd = params_for(len(q), max(int(off[-1]), 1), max(len(seqs), 1), **override)
+            tb = ps.traceback(q, p)
+            tref = oracle.traceback_hsps(q, res, off, ref, pd)
+            assert len(tb) == len(tref), f"seed {seed}: traceback count"
+            for f in TB_FIELDS:
+                assert tb[f].tolist() == [r[f] for r in tref], f"seed {seed}: traceback field {f}"
+        if rng.random() < 0.35:
+            qs = [q] + [synth.random_residues(rng, int(rng.integers(1, 1500))) for _ in range(int(rng.integers(1, 6)))]
+            plist, plain = [], []
+            for qq in qs:
+                p, _ = params_for(len(qq), max(int(off[-1]), 1), max(len(seqs), 1), **override)
+                plist.append(p)
+                qh = blaze103.Query(db, qq, p.word_threshold)
+                try:
+                    ps.run_query(qh, p)
+                    plain.append(ps.results())
+                finally:
+                    qh.close()
+            b = blaze103.QueryBatch(db, qs, plist[0].word_threshold)
+            try:
+                out = ps.run_batch(b, plist)
+            finally:
+                b.close()
+            for i, pr in enumerate(plain):
+                mine = out[out["query"] == i]
+                for f in ("oid", "score", "q_start", "q_end", "s_start", "s_end"):
+                    assert np.array_equal(mine[f], pr[f]), f"seed {seed}: batch query {i} field {f}"
+    finally:
+        ps.close()
+        db.close()
+
+
+@pytest.mark.parametrize("block", range(10))
+def test_random_cases(block):
+    for seed in range(1000 + 30 * block, 1000 + 30 * (block + 1)):
+        run_case(seed)
