@@ -75,6 +75,7 @@ extern "C" int blaze_db_create(int device, const uint8_t *residues, const uint64
     do {
         cudaError_t e = cudaMalloc(&db->d_res, total + 64);
         if (e == cudaSuccess) e = cudaMalloc(&db->d_off, sizeof(uint64_t) * (n_subjects + 1));
+        if (e == cudaSuccess) e = cudaMalloc(&db->d_oid, sizeof(uint32_t) * std::max<uint32_t>(n_subjects, 1));
         if (e != cudaSuccess) {
             last_cuda_error(e);
             rc = e == cudaErrorMemoryAllocation ? BLAZE_ERR_OUT_OF_MEMORY : BLAZE_ERR_CUDA;
@@ -90,6 +91,8 @@ extern "C" int blaze_db_create(int device, const uint8_t *residues, const uint64
         }
         if (e == cudaSuccess) e = cudaMemset(db->d_res + total, 0, 64);
         if (e == cudaSuccess) e = cudaMemcpy(db->d_off, off.data(), sizeof(uint64_t) * (n_subjects + 1), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && n_subjects)
+            e = cudaMemcpy(db->d_oid, order.data(), sizeof(uint32_t) * n_subjects, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) {
             last_cuda_error(e);
             rc = BLAZE_ERR_CUDA;
@@ -109,6 +112,7 @@ extern "C" int blaze_db_free(blaze_db *db) {
     cudaSetDevice(db->device);
     if (db->d_res) cudaFree(db->d_res);
     if (db->d_off) cudaFree(db->d_off);
+    if (db->d_oid) cudaFree(db->d_oid);
     delete db;
     return BLAZE_OK;
 }
@@ -232,15 +236,24 @@ extern "C" int blaze_search_free(blaze_search *s) {
     s->bqlen.release();
     s->bcut.release();
     s->work_query.release();
-    s->out_query.release();
     s->cursors.release();
+    s->bsmin.release();
+    s->bmaxh.release();
+    s->sel_limit.release();
+    s->groups.release();
+    s->qkept.release();
+    s->seg_off.release();
+    s->seg_fill.release();
+    s->seg_idx.release();
+    s->sel_q.release();
+    s->seg_keys.release();
     s->tb_items.release();
     s->tb_out.release();
     s->tb_dirs.release();
     s->tb_rows.release();
     s->tb_dp.release();
     s->tb_cursor.release();
-    if (s->h_outq) cudaFreeHost(s->h_outq);
+    if (s->h_groups) cudaFreeHost(s->h_groups);
     if (s->d_cnt) cudaFree(s->d_cnt);
     if (s->h_cnt) cudaFreeHost(s->h_cnt);
     if (s->h_out) cudaFreeHost(s->h_out);
@@ -256,7 +269,29 @@ int check_params(const blaze_params *p) {
     if (p->window <= 0 || p->window > (1 << 20) || p->ungapped_xdrop <= 0 || p->gap_open < 0 ||
         p->gap_extend <= 0 || p->gapped_xdrop <= 0 || p->gapped_cutoff <= 0 || p->ungapped_cutoff <= 0)
         return BLAZE_ERR_INVALID_ARG;
+    // E-value statistics: E must fall with the score (the reap is a score threshold)
+    if (!(p->lambda > 0.0) || !std::isfinite(p->lambda) || !(p->K > 0.0) || !std::isfinite(p->K) ||
+        !(p->eff_searchsp >= 0.0) || !std::isfinite(p->eff_searchsp) || std::isnan(p->prelim_evalue))
+        return BLAZE_ERR_INVALID_ARG;
     return BLAZE_OK;
+}
+
+// The preliminary reap drops an HSP when eff_searchsp * K * exp(-lambda * S)
+// exceeds prelim_evalue. E falls with S, so on the scores a gapped HSP can
+// have (1 and up) it keeps exactly those from the smallest passing S, found
+// by bisection over the same expression.
+static int32_t reap_min_score(const blaze_params &p) {
+    auto keeps = [&p](int64_t S) {
+        return !(p.eff_searchsp * p.K * std::exp(-p.lambda * static_cast<double>(S)) > p.prelim_evalue);
+    };
+    int64_t lo = 1, hi = INT32_MAX;  // keeps(hi) or no score passes
+    if (keeps(lo)) return 1;
+    if (!keeps(hi)) return INT32_MAX;
+    while (hi - lo > 1) {  // !keeps(lo), keeps(hi)
+        const int64_t mid = lo + (hi - lo) / 2;
+        (keeps(mid) ? hi : lo) = mid;
+    }
+    return static_cast<int32_t>(hi);
 }
 
 // What one run searches: one query, or a batch with one parameter set per
@@ -265,6 +300,7 @@ struct RunSpec {
     const blaze_query *q = nullptr;
     const blaze_batch *b = nullptr;
     const blaze_params *p = nullptr;
+    std::vector<int32_t> smin;  // per query: the reap's lowest kept score
 };
 
 // One pass of both stages; fills s->h_cnt.
@@ -424,10 +460,10 @@ static int run_pass(blaze_search *s, const RunSpec &r, const std::vector<ScanPla
     if ((rc = s->init_out.ensure(s->init_cap)) != BLAZE_OK) return rc;
     if ((rc = s->work.ensure(work_cap)) != BLAZE_OK) return rc;
     if ((rc = s->out.ensure(s->out_cap)) != BLAZE_OK) return rc;
-    if (batched) {
-        if ((rc = s->work_query.ensure(work_cap)) != BLAZE_OK) return rc;
-        if ((rc = s->out_query.ensure(s->out_cap)) != BLAZE_OK) return rc;
-    }
+    const uint32_t nq = batched ? r.b->n : 1u;
+    if ((rc = s->groups.ensure(s->out_cap)) != BLAZE_OK) return rc;  // a published list holds >= 1 HSP
+    if ((rc = s->qkept.ensure(nq)) != BLAZE_OK) return rc;
+    if (batched && (rc = s->work_query.ensure(work_cap)) != BLAZE_OK) return rc;
     const size_t dp_stride = static_cast<size_t>(std::max<uint32_t>(db->max_len, 1)) + 2;
     if ((rc = s->dp.ensure(gapped_warps * 2 * dp_stride)) != BLAZE_OK) return rc;
     if ((rc = s->cursors.ensure(plans.size())) != BLAZE_OK) return rc;
@@ -501,19 +537,26 @@ static int run_pass(blaze_search *s, const RunSpec &r, const std::vector<ScanPla
     ga.xdrop = p->gapped_xdrop;
     ga.out = s->out.p;
     ga.out_cap = s->out_cap;
+    ga.oid = db->d_oid;
+    ga.groups = s->groups.p;
+    ga.qkept = s->qkept.p;
     ga.cnt = s->d_cnt;
     if (batched) {
         ga.work_query = s->work_query.p;
         ga.batch_q = s->bqptr.p;
         ga.batch_qlen = s->bqlen.p;
         ga.batch_cutoff = s->bcut.p;
-        ga.out_query = s->out_query.p;
+        ga.batch_smin = s->bsmin.p;
+        ga.batch_max_hsps = s->bmaxh.p;
     } else {
         ga.q = r.q->d_q;
         ga.qlen = r.q->qlen;
         ga.cutoff = p->gapped_cutoff;
+        ga.smin = r.smin[0];
+        ga.max_hsps = p->max_hsps;
     }
     pl.ga = &ga;
+    BLAZE_CUDA_TRY(cudaMemsetAsync(s->qkept.p, 0, sizeof(uint32_t) * nq, s->stream));
     const bool graph = s->launch_mode == 2 || (s->launch_mode == 0 && batched);
     if ((rc = graph ? launch_pass_graph(s, pl) : launch_pass_direct(s, pl)) != BLAZE_OK) return rc;
     s->stats.kernel_launches += static_cast<uint32_t>(pl.scans.size()) + 1;
@@ -536,11 +579,14 @@ static int ensure_pinned(T *&p, size_t &n, size_t want) {
 // Runs both stages (growing buffers and repeating a pass that overflowed),
 // copies the HSPs back and finishes them: E-values, preliminary reap, order
 // by (query, OID).
-static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
+static int run_search(blaze_search *s, const RunSpec &spec, uint64_t *n_hsps) {
     blaze_db *db = s->db;
-    const blaze_params *p0 = r.p;
-    const bool batched = r.b != nullptr;
-    const uint32_t nq = batched ? r.b->n : 1;
+    const blaze_params *p0 = spec.p;
+    const bool batched = spec.b != nullptr;
+    const uint32_t nq = batched ? spec.b->n : 1;
+    RunSpec r = spec;
+    r.smin.resize(nq);
+    for (uint32_t i = 0; i < nq; ++i) r.smin[i] = reap_min_score(r.p[i]);
     s->results.clear();
     s->batch_results.clear();
     s->stats = blaze_stats{};
@@ -610,7 +656,7 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
         // batch order
         std::vector<BatchQuery> bq(nq);
         std::vector<const uint8_t *> qp(nq);
-        std::vector<int32_t> ql(nq), cut(nq);
+        std::vector<int32_t> ql(nq), cut(nq), mh(nq);
         for (uint32_t k = 0; k < nq; ++k) {
             const uint32_t i = order[k];
             const blaze_params &pi = r.p[i];
@@ -628,18 +674,23 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
             qp[i] = d.q;
             ql[i] = d.qlen;
             cut[i] = pi.gapped_cutoff;
+            mh[i] = pi.max_hsps;
         }
         int rc;
         if ((rc = s->bq.ensure(nq)) != BLAZE_OK) return rc;
         if ((rc = s->bqptr.ensure(nq)) != BLAZE_OK) return rc;
         if ((rc = s->bqlen.ensure(nq)) != BLAZE_OK) return rc;
         if ((rc = s->bcut.ensure(nq)) != BLAZE_OK) return rc;
+        if ((rc = s->bsmin.ensure(nq)) != BLAZE_OK) return rc;
+        if ((rc = s->bmaxh.ensure(nq)) != BLAZE_OK) return rc;
         BLAZE_CUDA_TRY(cudaMemcpyAsync(s->bq.p, bq.data(), sizeof(BatchQuery) * nq, cudaMemcpyHostToDevice, s->stream));
         BLAZE_CUDA_TRY(cudaMemcpyAsync(s->bqptr.p, qp.data(), sizeof(const uint8_t *) * nq, cudaMemcpyHostToDevice, s->stream));
         BLAZE_CUDA_TRY(cudaMemcpyAsync(s->bqlen.p, ql.data(), sizeof(int32_t) * nq, cudaMemcpyHostToDevice, s->stream));
         BLAZE_CUDA_TRY(cudaMemcpyAsync(s->bcut.p, cut.data(), sizeof(int32_t) * nq, cudaMemcpyHostToDevice, s->stream));
+        BLAZE_CUDA_TRY(cudaMemcpyAsync(s->bsmin.p, r.smin.data(), sizeof(int32_t) * nq, cudaMemcpyHostToDevice, s->stream));
+        BLAZE_CUDA_TRY(cudaMemcpyAsync(s->bmaxh.p, mh.data(), sizeof(int32_t) * nq, cudaMemcpyHostToDevice, s->stream));
         BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
-        s->stats.h2d_bytes += (sizeof(BatchQuery) + sizeof(const uint8_t *) + 2 * sizeof(int32_t)) * nq;
+        s->stats.h2d_bytes += (sizeof(BatchQuery) + sizeof(const uint8_t *) + 4 * sizeof(int32_t)) * nq;
     }
 
     DevCounters c{};
@@ -677,17 +728,64 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
         s->stats.reruns++;
     }
 
-    // copy back and finish on the host
+    // hit lists: a query keeping more subjects than its hitlist_size keeps
+    // the hitlist_size best on the device (the others' lists get n = 0)
+    const size_t n_groups = static_cast<size_t>(c.group_count);
+    bool limited = false;
+    for (uint32_t i = 0; i < nq; ++i) limited |= r.p[i].hitlist_size > 0;
+    if (limited && n_groups) {
+        std::vector<uint32_t> kept_per_query(nq);
+        BLAZE_CUDA_TRY(cudaMemcpyAsync(kept_per_query.data(), s->qkept.p, sizeof(uint32_t) * nq,
+                                       cudaMemcpyDeviceToHost, s->stream));
+        BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        s->stats.d2h_bytes += sizeof(uint32_t) * nq;
+        std::vector<uint32_t> seg(nq + 1, 0), sel;
+        std::vector<int32_t> limit(nq);
+        for (uint32_t i = 0; i < nq; ++i) {
+            limit[i] = r.p[i].hitlist_size;
+            const bool selects = limit[i] > 0 && kept_per_query[i] > static_cast<uint32_t>(limit[i]);
+            seg[i + 1] = seg[i] + (selects ? kept_per_query[i] : 0u);
+            if (selects) sel.push_back(i);
+        }
+        if (!sel.empty()) {
+            int rc2;
+            if ((rc2 = s->seg_off.ensure(nq + 1)) != BLAZE_OK) return rc2;
+            if ((rc2 = s->seg_fill.ensure(nq)) != BLAZE_OK) return rc2;
+            if ((rc2 = s->sel_limit.ensure(nq)) != BLAZE_OK) return rc2;
+            if ((rc2 = s->sel_q.ensure(sel.size())) != BLAZE_OK) return rc2;
+            if ((rc2 = s->seg_keys.ensure(seg[nq])) != BLAZE_OK) return rc2;
+            if ((rc2 = s->seg_idx.ensure(seg[nq])) != BLAZE_OK) return rc2;
+            BLAZE_CUDA_TRY(cudaMemcpyAsync(s->seg_off.p, seg.data(), sizeof(uint32_t) * (nq + 1),
+                                           cudaMemcpyHostToDevice, s->stream));
+            BLAZE_CUDA_TRY(cudaMemcpyAsync(s->sel_limit.p, limit.data(), sizeof(int32_t) * nq,
+                                           cudaMemcpyHostToDevice, s->stream));
+            BLAZE_CUDA_TRY(cudaMemcpyAsync(s->sel_q.p, sel.data(), sizeof(uint32_t) * sel.size(),
+                                           cudaMemcpyHostToDevice, s->stream));
+            BLAZE_CUDA_TRY(cudaMemsetAsync(s->seg_fill.p, 0, sizeof(uint32_t) * nq, s->stream));
+            s->stats.h2d_bytes += sizeof(uint32_t) * (nq + 1) + sizeof(int32_t) * nq + sizeof(uint32_t) * sel.size();
+            HitlistArgs ha{};
+            ha.groups = s->groups.p;
+            ha.n_groups = n_groups;
+            ha.seg_off = s->seg_off.p;
+            ha.seg_fill = s->seg_fill.p;
+            ha.keys = s->seg_keys.p;
+            ha.idx = s->seg_idx.p;
+            ha.sel_queries = s->sel_q.p;
+            ha.limit = s->sel_limit.p;
+            BLAZE_CUDA_TRY(launch_hitlist(ha, static_cast<uint32_t>(sel.size()), s->n_sm, s->stream));
+            s->stats.kernel_launches += 2;
+        }
+    }
+
+    // copy back: the kept HSPs and one descriptor per subject list
     const size_t n_out = static_cast<size_t>(c.out_count);
     if ((rc = ensure_pinned(s->h_out, s->h_out_n, n_out)) != BLAZE_OK) return rc;
-    if (batched && (rc = ensure_pinned(s->h_outq, s->h_outq_n, n_out)) != BLAZE_OK) return rc;
+    if ((rc = ensure_pinned(s->h_groups, s->h_groups_n, n_groups)) != BLAZE_OK) return rc;
     if (n_out) {
         BLAZE_CUDA_TRY(cudaMemcpyAsync(s->h_out, s->out.p, sizeof(DevHsp) * n_out, cudaMemcpyDeviceToHost, s->stream));
-        s->stats.d2h_bytes += sizeof(DevHsp) * n_out;
-        if (batched) {
-            BLAZE_CUDA_TRY(cudaMemcpyAsync(s->h_outq, s->out_query.p, sizeof(uint32_t) * n_out, cudaMemcpyDeviceToHost, s->stream));
-            s->stats.d2h_bytes += sizeof(uint32_t) * n_out;
-        }
+        BLAZE_CUDA_TRY(cudaMemcpyAsync(s->h_groups, s->groups.p, sizeof(GroupDesc) * n_groups,
+                                       cudaMemcpyDeviceToHost, s->stream));
+        s->stats.d2h_bytes += sizeof(DevHsp) * n_out + sizeof(GroupDesc) * n_groups;
     }
     BLAZE_CUDA_TRY(cudaEventRecord(s->ev[3], s->stream));
     BLAZE_CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -698,34 +796,25 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
         BLAZE_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev[0], s->ev[3]));
         s->stats.device_ms = ms;
     }
-    // groups: each (query, subject) list is contiguous and already in final order
-    struct Group { uint32_t query, oid; size_t first, n; };
-    auto query_of = [&](size_t i) { return batched ? s->h_outq[i] : 0u; };
-    std::vector<Group> groups;
-    for (size_t i = 0; i < n_out;) {
-        size_t j = i + 1;
-        while (j < n_out && s->h_out[j].subject == s->h_out[i].subject && query_of(j) == query_of(i)) ++j;
-        groups.push_back({query_of(i), s->db->oid_of[s->h_out[i].subject], i, j - i});
-        i = j;
-    }
-    std::sort(groups.begin(), groups.end(), [](const Group &a, const Group &b) {
-        return a.query != b.query ? a.query < b.query : a.oid < b.oid;
+    // the lists by (query, OID); E-values of the kept HSPs (the reap,
+    // max_hsps and the hit list already applied on the device)
+    std::vector<const GroupDesc *> order_g;
+    order_g.reserve(n_groups);
+    for (size_t i = 0; i < n_groups; ++i)
+        if (s->h_groups[i].n > 0) order_g.push_back(&s->h_groups[i]);
+    std::sort(order_g.begin(), order_g.end(), [](const GroupDesc *a, const GroupDesc *b) {
+        return a->query != b->query ? a->query < b->query : a->oid < b->oid;
     });
-    // E-values, the preliminary reap and per-subject max_hsps, then per query
-    // the hitlist_size subjects with the best E-values (a subject's best is
-    // its first HSP; ties by smaller OID), emitted in OID order
-    struct Kept { uint32_t query, oid; int32_t best; size_t first, n; };
-    std::vector<blaze_hsp> kept_hsps;
-    kept_hsps.reserve(n_out);
-    std::vector<Kept> kept;
-    for (const Group &g : groups) {
-        const blaze_params &pg = r.p[g.query];
-        const size_t first = kept_hsps.size();
-        for (size_t k = 0; k < g.n; ++k) {
-            if (pg.max_hsps > 0 && kept_hsps.size() - first >= static_cast<size_t>(pg.max_hsps)) break;
-            const DevHsp &d = s->h_out[g.first + k];
+    size_t n_keep = 0;
+    for (const GroupDesc *g : order_g) n_keep += g->n;
+    if (batched) s->batch_results.reserve(n_keep);
+    else s->results.reserve(n_keep);
+    for (const GroupDesc *g : order_g) {
+        const blaze_params &pg = r.p[g->query];
+        for (uint32_t k = 0; k < g->n; ++k) {
+            const DevHsp &d = s->h_out[g->first + k];
             blaze_hsp h;
-            h.oid = g.oid;
+            h.oid = g->oid;
             h.score = d.score;
             h.q_start = d.q_start;
             h.q_end = d.q_end;
@@ -734,47 +823,18 @@ static int run_search(blaze_search *s, const RunSpec &r, uint64_t *n_hsps) {
             h.q_gapped_start = d.q_gs;
             h.s_gapped_start = d.s_gs;
             h.evalue = pg.eff_searchsp * pg.K * std::exp(-pg.lambda * static_cast<double>(d.score));
-            if (h.evalue > pg.prelim_evalue) continue;  // preliminary E-value reap
-            kept_hsps.push_back(h);
-        }
-        if (kept_hsps.size() > first)
-            kept.push_back({g.query, g.oid, kept_hsps[first].score, first, kept_hsps.size() - first});
-    }
-    for (size_t i = 0; i < kept.size();) {  // hitlist per query
-        size_t j = i;
-        while (j < kept.size() && kept[j].query == kept[i].query) ++j;
-        const int32_t limit = r.p[kept[i].query].hitlist_size;
-        if (limit > 0 && j - i > static_cast<size_t>(limit)) {
-            std::vector<Kept> by_best(kept.begin() + i, kept.begin() + j);
-            std::sort(by_best.begin(), by_best.end(), [](const Kept &a, const Kept &b) {
-                return a.best != b.best ? a.best > b.best : a.oid < b.oid;
-            });
-            const Kept &cut = by_best[static_cast<size_t>(limit) - 1];
-            for (size_t k = i; k < j; ++k) {  // keep those ranked at or above the cut
-                const bool above = kept[k].best > cut.best || (kept[k].best == cut.best && kept[k].oid <= cut.oid);
-                if (!above) kept[k].n = 0;
-            }
-        }
-        i = j;
-    }
-    if (batched) s->batch_results.reserve(kept_hsps.size());
-    else s->results.reserve(kept_hsps.size());
-    uint32_t subjects = 0;
-    for (const Kept &k : kept) {
-        if (k.n == 0) continue;
-        ++subjects;
-        for (size_t t = 0; t < k.n; ++t) {
             if (batched) {
                 blaze_batch_hsp bh;
-                bh.query = k.query;
+                bh.query = g->query;
                 bh.reserved = 0;
-                bh.hsp = kept_hsps[k.first + t];
+                bh.hsp = h;
                 s->batch_results.push_back(bh);
             } else {
-                s->results.push_back(kept_hsps[k.first + t]);
+                s->results.push_back(h);
             }
         }
     }
+    const uint32_t subjects = static_cast<uint32_t>(order_g.size());
     const size_t n_res = batched ? s->batch_results.size() : s->results.size();
     s->last_init_count = c.init_count;
     s->last_work_count = c.work_count;

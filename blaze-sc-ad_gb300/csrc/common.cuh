@@ -63,6 +63,20 @@ struct DevCounters {
     unsigned int max_init_needed;    // largest init-hit count among those
     unsigned int flags;              // kFlag* bits
     unsigned int pad;
+    unsigned long long group_count;  // subject HSP lists published (GroupDesc records)
+};
+
+// One subject's HSP list in the gapped stage's output, after the preliminary
+// E-value reap and max_hsps: `n` HSPs from `first`, best first. The hit-list
+// selection sets n to 0 for a subject outside its query's hitlist_size.
+struct GroupDesc {
+    unsigned long long first;
+    uint32_t query;    // batched runs: the query's position in its batch
+    uint32_t subject;  // index into the length-sorted database
+    uint32_t oid;
+    uint32_t n;
+    int32_t best;      // score of the list's first HSP
+    uint32_t pad;
 };
 
 constexpr unsigned kFlagInitArrayFull = 1u;
@@ -123,7 +137,8 @@ struct GappedArgs {
     const uint8_t *const *batch_q;
     const int32_t *batch_qlen;
     const int32_t *batch_cutoff;
-    uint32_t *out_query;         // query index of each output HSP
+    const int32_t *batch_smin;       // per query: lowest score the preliminary reap keeps
+    const int32_t *batch_max_hsps;   // per query: HSPs kept per subject (0: all)
     const InitHit *init_in;
     const WorkItem *work;
     unsigned long long work_cap;
@@ -133,9 +148,27 @@ struct GappedArgs {
     int32_t *dp;         // per warp: 2 * dp_stride ints
     uint32_t dp_stride;  // >= max subject length + 2
     int32_t gap_open, gap_extend, xdrop, cutoff;
+    int32_t smin, max_hsps;  // single query: as batch_smin / batch_max_hsps
     DevHsp *out;
     unsigned long long out_cap;
+    const uint32_t *oid;     // sorted index -> OID
+    GroupDesc *groups;       // one per published list (null: none written)
+    uint32_t *qkept;         // per query: lists published (null: not counted)
     DevCounters *cnt;
+};
+
+// Hit-list selection: queries that keep more subjects than their
+// hitlist_size keep the hitlist_size best (score of the first HSP
+// descending, ties by smaller OID); the others' lists are marked n = 0.
+struct HitlistArgs {
+    GroupDesc *groups;
+    unsigned long long n_groups;
+    const uint32_t *seg_off;         // per query: its segment of keys (n_queries + 1; empty if not selecting)
+    uint32_t *seg_fill;              // per query: segment cursor, zeroed
+    unsigned long long *keys;        // segment storage: ranking key and list index
+    uint32_t *idx;
+    const uint32_t *sel_queries;     // the selecting queries, one block each
+    const int32_t *limit;            // per query: hitlist_size
 };
 
 // Shared-memory layout of the scan kernel for one query.
@@ -185,6 +218,7 @@ cudaError_t launch_scan(const ScanArgs &a, int n_blocks, int warps_per_block, si
 cudaError_t scan_occupancy(bool query_in_smem, int warps_per_block, size_t smem, int *blocks_per_sm);
 int scan_max_warps_by_registers(bool query_in_smem);
 cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st);
+cudaError_t launch_hitlist(const HitlistArgs &a, uint32_t n_select, int n_sm, cudaStream_t st);
 constexpr int kTracebackWarpsPerBlock = 4;
 cudaError_t launch_traceback(const TracebackArgs &a, int n_blocks, cudaStream_t st);
 cudaError_t launch_scan_batch(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem, cudaStream_t st);

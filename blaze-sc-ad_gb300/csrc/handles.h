@@ -20,6 +20,7 @@ struct blaze_db {
     int device = 0;
     uint8_t *d_res = nullptr;
     uint64_t *d_off = nullptr;
+    uint32_t *d_oid = nullptr;     // sorted index -> OID (the hit-list tie rule)
     uint64_t total = 0;
     uint32_t n = 0;
     uint32_t max_len = 0;
@@ -99,10 +100,16 @@ struct blaze_search {
     DevBuf<BatchQuery> bq;
     DevBuf<const uint8_t *> bqptr;
     DevBuf<int32_t> bqlen, bcut;
-    DevBuf<uint32_t> work_query, out_query;
+    DevBuf<uint32_t> work_query;
     DevBuf<unsigned long long> cursors;  // one work cursor per scan launch of a pass
-    uint32_t *h_outq = nullptr;  // pinned
-    size_t h_outq_n = 0;
+    // per-query finishing on the device: reap score, max_hsps, published
+    // lists per query, and the hit-list selection's segments
+    DevBuf<int32_t> bsmin, bmaxh, sel_limit;
+    DevBuf<GroupDesc> groups;
+    DevBuf<uint32_t> qkept, seg_off, seg_fill, seg_idx, sel_q;
+    DevBuf<unsigned long long> seg_keys;
+    GroupDesc *h_groups = nullptr;  // pinned
+    size_t h_groups_n = 0;
     std::vector<blaze_batch_hsp> batch_results;
     // traceback stage
     DevBuf<TbItem> tb_items;

@@ -5,11 +5,15 @@
 //   gapped_kernel  one warp per work item: orders the init hits, skips those
 //                  contained in kept HSPs, runs the left and right score-only
 //                  X-drop DP row-parallel across the warp, then purges common
-//                  endpoints and sorts the subject's HSP list.
+//                  endpoints, sorts the subject's HSP list and keeps what the
+//                  preliminary reap and max_hsps keep.
+//   hitlist_*      per query, the hitlist_size best subject lists (radix
+//                  select on the device).
 //
 // Reference counterpart: gpuBLAZE_everything (BLAZE_gpu/gpuBLAZE.cu:1254-1397);
 // unlike that filter (whose survivors the CPU re-searches) this kernel
 // produces the final HSPs.
+#include <algorithm>
 #include <cstdint>
 
 #include "common.cuh"
@@ -268,6 +272,8 @@ gapped_kernel(const GappedArgs a) {
         const uint8_t *qres = a.work_query ? a.batch_q[qi] : a.q;
         const int32_t qlen = a.work_query ? a.batch_qlen[qi] : a.qlen;
         const int32_t cutoff = a.work_query ? a.batch_cutoff[qi] : a.cutoff;
+        const int32_t smin = a.work_query ? a.batch_smin[qi] : a.smin;
+        const int32_t max_hsps = a.work_query ? a.batch_max_hsps[qi] : a.max_hsps;
         const uint32_t n = wi.n_init;
         const InitHit *in = a.init_in + wi.first;
         const uint64_t o0 = a.off[wi.subject];
@@ -324,8 +330,15 @@ gapped_kernel(const GappedArgs a) {
             }
             __syncwarp();
         }
+        // purge and order; then the preliminary E-value reap (E-values fall
+        // with the score, so it keeps the leading HSPs scoring at least smin)
+        // and at most max_hsps of them
         int m = 0;
-        if (lane == 0) m = purge_and_sort(saved, nsaved);
+        if (lane == 0) {
+            const int all = purge_and_sort(saved, nsaved);
+            while (m < all && saved[m].score >= smin) ++m;
+            if (max_hsps > 0 && m > max_hsps) m = max_hsps;
+        }
         m = __shfl_sync(kFull, m, 0);
         __syncwarp();
         if (m > 0) {
@@ -335,9 +348,21 @@ gapped_kernel(const GappedArgs a) {
             if (base + m > a.out_cap) {
                 if (lane == 0) atomicOr(&a.cnt->flags, kFlagOutArrayFull);
             } else {
-                for (int i = lane; i < m; i += 32) {
-                    a.out[base + i] = saved[i];
-                    if (a.out_query) a.out_query[base + i] = qi;
+                for (int i = lane; i < m; i += 32) a.out[base + i] = saved[i];
+                if (lane == 0 && a.groups) {
+                    // every published list holds at least one of the out_cap
+                    // HSPs, so the descriptor index stays below out_cap
+                    const unsigned long long gi = atomicAdd(&a.cnt->group_count, 1ull);
+                    GroupDesc g;
+                    g.first = base;
+                    g.query = qi;
+                    g.subject = wi.subject;
+                    g.oid = a.oid[wi.subject];
+                    g.n = static_cast<uint32_t>(m);
+                    g.best = saved[0].score;
+                    g.pad = 0;
+                    a.groups[gi] = g;
+                    if (a.qkept) atomicAdd(&a.qkept[qi], 1u);
                 }
             }
         }
@@ -348,7 +373,77 @@ gapped_kernel(const GappedArgs a) {
     }
 }
 
+// ------------------------------------------------------------------------
+// Hit-list selection (hitlist_size, max_target_seqs), for the queries whose
+// kept subjects outnumber their limit. The ranking key orders subjects by
+// the score of their best HSP, then by smaller OID; keys within a query are
+// distinct, so the k-th largest key is exact and exactly k lists stay.
+
+__device__ __forceinline__ unsigned long long rank_key(const GroupDesc &g) {
+    return (static_cast<unsigned long long>(static_cast<uint32_t>(g.best) ^ 0x80000000u) << 32) |
+           static_cast<unsigned long long>(0xffffffffu - g.oid);
+}
+
+// Lays each selecting query's keys out in its own segment.
+__global__ void hitlist_scatter_kernel(const HitlistArgs a) {
+    for (unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+         g < a.n_groups; g += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        const GroupDesc d = a.groups[g];
+        const uint32_t lo = a.seg_off[d.query], hi = a.seg_off[d.query + 1];
+        if (hi == lo) continue;
+        const uint32_t pos = lo + atomicAdd(&a.seg_fill[d.query], 1u);
+        if (pos >= hi) continue;  // cannot happen: the segment holds the query's published lists
+        a.keys[pos] = rank_key(d);
+        a.idx[pos] = static_cast<uint32_t>(g);
+    }
+}
+
+// One block per selecting query: an MSB-first radix select (8-bit digits)
+// finds the limit-th largest key; lists below it are dropped.
+__global__ void __launch_bounds__(256) hitlist_select_kernel(const HitlistArgs a) {
+    __shared__ uint32_t hist[256];
+    __shared__ unsigned long long s_prefix;
+    __shared__ uint32_t s_rank;
+    const uint32_t q = a.sel_queries[blockIdx.x];
+    const uint32_t lo = a.seg_off[q], hi = a.seg_off[q + 1];
+    unsigned long long prefix = 0, mask = 0;
+    uint32_t rank = static_cast<uint32_t>(a.limit[q]);  // 1 <= rank < hi - lo
+    for (int shift = 56; shift >= 0; shift -= 8) {
+        for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+        __syncthreads();
+        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+            const unsigned long long k = a.keys[i];
+            if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 0xffu], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t above = 0;
+            int b = 255;
+            for (; b > 0 && above + hist[b] < rank; --b) above += hist[b];
+            s_prefix = prefix | (static_cast<unsigned long long>(b) << shift);
+            s_rank = rank - above;
+        }
+        __syncthreads();
+        prefix = s_prefix;
+        rank = s_rank;
+        mask |= 0xffull << shift;
+    }
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+        if (a.keys[i] < prefix) a.groups[a.idx[i]].n = 0u;
+}
+
 }  // namespace
+
+cudaError_t launch_hitlist(const HitlistArgs &a, uint32_t n_select, int n_sm, cudaStream_t st) {
+    if (a.n_groups == 0 || n_select == 0) return cudaSuccess;
+    const unsigned long long want = (a.n_groups + 255) / 256;
+    const int blocks = static_cast<int>(std::min<unsigned long long>(want, static_cast<unsigned long long>(n_sm) * 8));
+    hitlist_scatter_kernel<<<blocks, 256, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    hitlist_select_kernel<<<n_select, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st) {
     gapped_kernel<<<n_blocks, kGappedWarpsPerBlock * 32, 0, st>>>(a);

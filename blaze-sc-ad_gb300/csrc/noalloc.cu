@@ -105,6 +105,8 @@ extern "C" int blaze_gapped_noalloc(const uint8_t *d_residues, const uint64_t *d
     ga.gap_extend = p->gap_extend;
     ga.xdrop = p->gapped_xdrop;
     ga.cutoff = p->gapped_cutoff;
+    ga.smin = INT32_MIN;  // every HSP of each list: this entry point reports raw HSPs
+    ga.max_hsps = 0;
     ga.out = reinterpret_cast<DevHsp *>(d_out);
     ga.out_cap = out_capacity;
     ga.cnt = cnt;

@@ -66,9 +66,11 @@ typedef struct blaze_params {
     double K;                /* gapped Karlin-Altschul K */
     double eff_searchsp;     /* effective search space of the query */
     double prelim_evalue;    /* HSPs with a larger E-value are dropped */
-    /* Culling of the returned lists (0: none). hitlist_size (NCBI
-     * max_target_seqs): per query, the subjects with the best E-values, ties
-     * by smaller OID. max_hsps: per subject, the first HSPs of its list. */
+    /* Culling of the returned lists, on the device (0: none). hitlist_size
+     * (NCBI max_target_seqs): per query, the subjects with the best E-values,
+     * ties by smaller OID. max_hsps: per subject, the first HSPs of its list.
+     * lambda, K and eff_searchsp must be finite with lambda, K > 0 and
+     * eff_searchsp >= 0 (BLAZE_ERR_INVALID_ARG otherwise). */
     int32_t hitlist_size;
     int32_t max_hsps;
 } blaze_params;

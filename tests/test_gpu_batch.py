@@ -143,3 +143,33 @@ def test_graph_replay_matches_direct_launches():
     batch.close()
     ps.close()
     db.close()
+
+
+def test_batch_culling_per_query():
+    # hitlist_size, max_hsps and the preliminary reap differ per query; each
+    # query's records equal its plain run with the same parameters, and the
+    # plain run equals the oracle's reap and culling
+    qs = _queries()
+    res, off = _db(with_homologs_of=qs)
+    db = blaze103.SeqSrc(res, off)
+    ps = blaze103.PrelimSearch(db)
+    settings = [dict(hitlist_size=3), dict(max_hsps=1), dict(prelim_evalue=1e-3), {},
+                dict(hitlist_size=5, max_hsps=2, prelim_evalue=0.5), dict(hitlist_size=1),
+                dict(hitlist_size=100000), dict(prelim_evalue=1e-30), dict(max_hsps=3), dict(hitlist_size=2)]
+    params = [params_for(len(q), db.tot_len, db.num_seqs, **k)[0] for q, k in zip(qs, settings)]
+    want = [_plain(ps, db, q, p) for q, p in zip(qs, params)]
+    batch = blaze103.QueryBatch(db, qs)
+    got = ps.run_batch(batch, params)
+    for i, w in enumerate(want):
+        g = got[got["query"] == i]
+        for f in blaze103.HSP_DTYPE.names:
+            assert np.array_equal(g[f], w[f]), (i, f)
+    for i in (0, 4):
+        pd = params_for(len(qs[i]), int(off[-1]), len(off) - 1, **settings[i])[1]
+        ref, _ = oracle_run(qs[i], res, off, pd)
+        assert np.array_equal(want[i]["oid"], ref["subject"])
+        assert np.array_equal(want[i]["score"], ref["score"])
+    assert len(np.unique(got[got["query"] == 0]["oid"])) <= 3
+    batch.close()
+    ps.close()
+    db.close()

@@ -146,7 +146,8 @@ def test_query_longer_than_shared_copy():
 
 
 @pytest.mark.parametrize("cull", [dict(hitlist_size=7), dict(max_hsps=1), dict(hitlist_size=3, max_hsps=2),
-                                  dict(hitlist_size=100000)])
+                                  dict(hitlist_size=100000), dict(prelim_evalue=1e-3),
+                                  dict(prelim_evalue=1e-6, hitlist_size=4, max_hsps=1), dict(hitlist_size=1)])
 def test_hitlist_culling(cull):
     rng = np.random.default_rng(77)
     q = synth.random_residues(rng, 400)
@@ -159,7 +160,7 @@ def test_hitlist_culling(cull):
             seqs[i] = np.concatenate([seqs[i][:pos], hom, seqs[i][pos:]])
     res, off = concat(seqs)
     got, ref, _ = compare(q, res, off, **cull)
-    full, _, _ = compare(q, res, off)
+    full, _, _ = compare(q, res, off, **{k: v for k, v in cull.items() if k == "prelim_evalue"})
     assert len(got) > 0
     if "hitlist_size" in cull:
         assert len(set(got["oid"].tolist())) == min(cull["hitlist_size"], len(set(full["oid"].tolist())))

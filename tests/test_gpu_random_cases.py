@@ -82,6 +82,12 @@ def make_case(rng):
     if rng.random() < 0.3:
         tuning = dict(stage_bytes=int(rng.choice([0, 128, 256, 4096, 16384])),
                       max_warps_per_block=int(rng.choice([0, 1, 4, 13, 32])))
+    if rng.random() < 0.15:
+        override["hitlist_size"] = int(rng.choice([1, 2, 5, 20]))
+    if rng.random() < 0.1:
+        override["max_hsps"] = int(rng.choice([1, 2, 4]))
+    if rng.random() < 0.1:
+        override["prelim_evalue"] = float(rng.choice([1e-6, 0.01, 1.0]))
     return q, seqs, override, tuning
 
 
