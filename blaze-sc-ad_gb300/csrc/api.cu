@@ -527,6 +527,9 @@ static int run_pass(blaze_search *s, const RunSpec &r, const std::vector<ScanPla
     ga.init_in = s->init_out.p;
     ga.work = s->work.p;
     ga.work_cap = work_cap;
+    ga.init_cap = s->init_cap;
+    ga.n_subj = db->n;
+    ga.n_queries = nq;
     ga.sorted = s->sorted.p;
     ga.saved = s->saved.p;
     ga.cap = s->scratch_cap;

@@ -142,6 +142,8 @@ struct GappedArgs {
     const InitHit *init_in;
     const WorkItem *work;
     unsigned long long work_cap;
+    unsigned long long init_cap;  // records in init_in (items beyond it are rejected)
+    uint32_t n_subj, n_queries;   // valid subject and query indices of an item
     InitHit *sorted;     // per warp: cap records
     DevHsp *saved;       // per warp: cap records
     uint32_t cap;

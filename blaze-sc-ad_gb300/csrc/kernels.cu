@@ -260,7 +260,12 @@ gapped_kernel(const GappedArgs a) {
     int32_t *Hb = a.dp + gwarp * 2ull * a.dp_stride;
     int32_t *Eb = Hb + a.dp_stride;
     unsigned long long n_work = *reinterpret_cast<volatile unsigned long long *>(&a.cnt->work_count);
-    if (n_work > a.work_cap) n_work = a.work_cap;  // an overflowed run is repeated by the host
+    if (n_work > a.work_cap) n_work = a.work_cap;
+    // A scan that overflowed its init-hit or work array counted items it
+    // could not write; the host repeats that pass with larger arrays, so this
+    // one takes no work at all (an unwritten slot holds no valid item).
+    const unsigned scan_flags = *reinterpret_cast<volatile unsigned *>(&a.cnt->flags);
+    if (scan_flags & (kFlagInitArrayFull | kFlagWorkArrayFull | kFlagBadState)) n_work = 0;
     unsigned long long cells = 0, n_ext = 0;
     for (;;) {
         unsigned long long t = 0;
@@ -269,6 +274,11 @@ gapped_kernel(const GappedArgs a) {
         if (t >= n_work) break;
         const WorkItem wi = a.work[t];
         const uint32_t qi = a.work_query ? a.work_query[t] : 0u;
+        if (wi.subject >= a.n_subj || qi >= a.n_queries || wi.first > a.init_cap ||
+            wi.n_init > a.init_cap - wi.first) {  // cannot happen: every counted item is written
+            if (lane == 0) atomicOr(&a.cnt->flags, kFlagBadState);
+            continue;
+        }
         const uint8_t *qres = a.work_query ? a.batch_q[qi] : a.q;
         const int32_t qlen = a.work_query ? a.batch_qlen[qi] : a.qlen;
         const int32_t cutoff = a.work_query ? a.batch_cutoff[qi] : a.cutoff;

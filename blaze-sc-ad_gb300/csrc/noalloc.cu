@@ -96,6 +96,9 @@ extern "C" int blaze_gapped_noalloc(const uint8_t *d_residues, const uint64_t *d
     ga.init_in = reinterpret_cast<const InitHit *>(d_init_hits);
     ga.work = reinterpret_cast<const WorkItem *>(d_subjects);
     ga.work_cap = n_subjects;
+    ga.init_cap = ~0ull;  // the caller's arrays: sizes unknown here
+    ga.n_subj = ~0u;
+    ga.n_queries = 1;
     ga.sorted = reinterpret_cast<InitHit *>(base + kCountersBytes);
     ga.saved = reinterpret_cast<DevHsp *>(base + kCountersBytes + kSortedBytes);
     ga.cap = kMaxInit;

@@ -603,8 +603,17 @@ __device__ __forceinline__ void process_subject(Finder &f, const ScanArgs &a, co
             first = __shfl_sync(kFull, first, 0);
             wi = __shfl_sync(kFull, wi, 0);
             if (first + f.n_init > a.init_cap || wi >= a.work_cap) {
-                if (lane == 0)
+                if (lane == 0) {
                     atomicOr(&a.cnt->flags, first + f.n_init > a.init_cap ? kFlagInitArrayFull : kFlagWorkArrayFull);
+                    if (wi < a.work_cap) {  // a counted slot always holds an item: an empty one
+                        WorkItem w;
+                        w.subject = subj;
+                        w.n_init = 0;
+                        w.first = 0;
+                        a.work[wi] = w;
+                        if (a.work_query) a.work_query[wi] = query_index;
+                    }
+                }
             } else {
                 for (uint32_t i = lane; i < f.n_init; i += 32) a.init_out[first + i] = f.scratch[i];
                 if (lane == 0) {

@@ -139,3 +139,15 @@ def run_case(seed):
 def test_random_cases(block):
     for seed in range(1000 + 30 * block, 1000 + 30 * (block + 1)):
         run_case(seed)
+
+
+def test_random_cases_with_tiny_buffers(monkeypatch):
+    # every buffer starts tiny, so passes overflow and repeat with larger
+    # ones; a scan pass that overflowed its init-hit array counted work items
+    # it could not write, and the gapped stage of that pass must take none of
+    # them (seed 200131 is such a case)
+    for k, v in dict(BLAZE_INITIAL_SCRATCH_CAP=4, BLAZE_INITIAL_INIT_CAP=16, BLAZE_INITIAL_OUT_CAP=8,
+                     BLAZE_INITIAL_WORK_CAP=8, BLAZE_INITIAL_TRACEBACK_CAP=64).items():
+        monkeypatch.setenv(k, str(v))
+    for seed in range(200000, 200140):
+        run_case(seed)
