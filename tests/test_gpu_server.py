@@ -4,6 +4,7 @@ queries and is batched with them, whatever the number of batches in flight,
 the batch size or the memory budget; two of them are checked against the
 oracle as well."""
 import threading
+import time
 
 import numpy as np
 import pytest
@@ -131,3 +132,49 @@ def test_concurrent_search_contexts(served):
     for t in threads:
         t.join()
     assert errors == []
+
+
+@pytest.mark.parametrize("seed", range(7000, 7012))
+def test_random_server_settings(seed):
+    # random slots, batch cap, memory budget (down to 1 byte: one query at a
+    # time next to a running batch), batching window, launch mode and tile
+    # size; queries from three threads with random gaps; each result equals
+    # the query's plain run
+    rng = np.random.default_rng(seed)
+    seqs = [synth.random_residues(rng, int(L))
+            for L in synth.lognormal_lengths(rng, int(rng.choice([50, 500])), 250, 0.9, 1, 4000)]
+    qs = [synth.random_residues(rng, int(rng.integers(1, 3000))) for _ in range(int(rng.integers(1, 40)))]
+    for i in range(0, len(seqs), 5):
+        q = qs[int(rng.integers(0, len(qs)))]
+        if len(q) > 30:
+            w = min(len(q), int(rng.integers(30, 300)))
+            s0 = int(rng.integers(0, len(q) - w + 1))
+            seqs[i] = np.concatenate([seqs[i], synth.mutate(rng, q[s0:s0 + w], 0.5)])
+    res, off = concat(seqs)
+    db = blaze103.SeqSrc(res, off)
+    ps = blaze103.PrelimSearch(db, autotune=False)
+    want = [ps.run(q).hsps for q in qs]
+    ps.close()
+    srv = blaze103.Server(db, slots=int(rng.integers(1, 5)), max_batch=int(rng.choice([1, 2, 7, 64])),
+                          memory_budget=int(rng.choice([0, 1, 1 << 20, 64 << 20])),
+                          batch_window_us=int(rng.choice([0, 100, 2000])),
+                          tuning=dict(launch_mode=int(rng.integers(0, 3)), tile_residues=int(rng.choice([0, 1, 4096]))))
+    tickets = [None] * len(qs)
+    gaps = rng.exponential(0.0005, len(qs))
+
+    def submit(idx):
+        for i in idx:
+            time.sleep(float(gaps[i]))
+            tickets[i] = srv.submit(qs[i])
+
+    threads = [threading.Thread(target=submit, args=(list(range(k, len(qs), 3)),)) for k in range(3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for i, tk in enumerate(tickets):
+        got = srv.wait(tk, 60000)
+        for f in blaze103.HSP_DTYPE.names:
+            assert np.array_equal(got[f], want[i][f]), (i, f)
+    srv.close()
+    db.close()
