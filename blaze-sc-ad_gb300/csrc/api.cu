@@ -125,6 +125,35 @@ extern "C" int blaze_db_info(const blaze_db *db, uint64_t *total, uint32_t *n, u
     return BLAZE_OK;
 }
 
+// A query's word tables on the host: cell_start (kWords + 1 prefix offsets),
+// the packed cells (start << 8 | min(count, 255); 255: look at cell_start),
+// the word-presence bitset and the hit lists (query offsets).
+struct QueryTables {
+    std::vector<uint32_t> cs, pack, pres;
+    uint16_t *offs = nullptr;  // malloc'd by build_lookup
+    uint32_t n_off = 0;
+    ~QueryTables() { std::free(offs); }
+};
+
+static int query_tables(const uint8_t *query, int32_t length, int32_t word_threshold, QueryTables &t) {
+    t.cs.assign(kWords + 1, 0u);
+    int rc = build_lookup(query, length, word_threshold, t.cs.data(), &t.offs, &t.n_off);
+    if (rc != BLAZE_OK) return rc;
+    t.pack.assign(kWords, 0u);
+    t.pres.assign(kPresenceWords, 0u);
+    for (int w = 0; w < kWords; ++w) {
+        const uint32_t cnt = t.cs[w + 1] - t.cs[w];
+        t.pack[w] = (t.cs[w] << 8) | std::min<uint32_t>(cnt, 255u);
+        if (cnt) t.pres[w >> 5] |= 1u << (w & 31);
+    }
+    return BLAZE_OK;
+}
+
+static uint64_t query_upload_bytes(int32_t length, uint32_t n_off) {
+    return static_cast<uint64_t>(length) + sizeof(uint32_t) * (2 * kWords + 1 + kPresenceWords) +
+           sizeof(uint16_t) * n_off;
+}
+
 extern "C" int blaze_query_create(const blaze_db *db, const uint8_t *query, int32_t length,
                                   int32_t word_threshold, blaze_query **out) {
     if (!db || !query || !out || length <= 0) return BLAZE_ERR_INVALID_ARG;
@@ -132,38 +161,26 @@ extern "C" int blaze_query_create(const blaze_db *db, const uint8_t *query, int3
     if (length > kMaxQueryLength) return BLAZE_ERR_LIMIT;
     if (!valid_residues(query, static_cast<uint64_t>(length))) return BLAZE_ERR_INVALID_ARG;
     BLAZE_CUDA_TRY(cudaSetDevice(db->device));
-    std::vector<uint32_t> cs(kWords + 1);
-    uint16_t *offs = nullptr;
-    uint32_t n_off = 0;
-    int rc = build_lookup(query, length, word_threshold, cs.data(), &offs, &n_off);
+    QueryTables t;
+    int rc = query_tables(query, length, word_threshold, t);
     if (rc != BLAZE_OK) return rc;
     auto *q = new blaze_query();
     q->device = db->device;
     q->qlen = length;
     q->threshold = word_threshold;
-    q->n_off = n_off;
+    q->n_off = t.n_off;
     cudaError_t e = cudaMalloc(&q->d_q, static_cast<size_t>(length) + 64);
     if (e == cudaSuccess) e = cudaMalloc(&q->d_cell_start, sizeof(uint32_t) * (kWords + 1));
-    if (e == cudaSuccess) e = cudaMalloc(&q->d_cell_off, sizeof(uint16_t) * std::max<uint32_t>(n_off, 1));
-    // packed cells (start << 8 | count, 255 = look at cell_start) and the
-    // word-presence bitset of the scan kernel
-    std::vector<uint32_t> pack(kWords), pres(kPresenceWords, 0u);
-    for (int w = 0; w < kWords; ++w) {
-        const uint32_t cnt = cs[w + 1] - cs[w];
-        pack[w] = (cs[w] << 8) | std::min<uint32_t>(cnt, 255u);
-        if (cnt) pres[w >> 5] |= 1u << (w & 31);
-    }
+    if (e == cudaSuccess) e = cudaMalloc(&q->d_cell_off, sizeof(uint16_t) * std::max<uint32_t>(t.n_off, 1));
     if (e == cudaSuccess) e = cudaMalloc(&q->d_cell_pack, sizeof(uint32_t) * kWords);
     if (e == cudaSuccess) e = cudaMalloc(&q->d_presence, sizeof(uint32_t) * kPresenceWords);
-    if (e == cudaSuccess) e = cudaMemcpy(q->d_cell_pack, pack.data(), sizeof(uint32_t) * kWords, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(q->d_presence, pres.data(), sizeof(uint32_t) * kPresenceWords, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(q->d_cell_pack, t.pack.data(), sizeof(uint32_t) * kWords, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(q->d_presence, t.pres.data(), sizeof(uint32_t) * kPresenceWords, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(q->d_q, query, length, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(q->d_q + length, 0, 64);
-    if (e == cudaSuccess) e = cudaMemcpy(q->d_cell_start, cs.data(), sizeof(uint32_t) * (kWords + 1), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && n_off) e = cudaMemcpy(q->d_cell_off, offs, sizeof(uint16_t) * n_off, cudaMemcpyHostToDevice);
-    std::free(offs);
-    q->upload_bytes = static_cast<uint64_t>(length) + sizeof(uint32_t) * (2 * kWords + 1 + kPresenceWords) +
-                      sizeof(uint16_t) * n_off;
+    if (e == cudaSuccess) e = cudaMemcpy(q->d_cell_start, t.cs.data(), sizeof(uint32_t) * (kWords + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && t.n_off) e = cudaMemcpy(q->d_cell_off, t.offs, sizeof(uint16_t) * t.n_off, cudaMemcpyHostToDevice);
+    q->upload_bytes = query_upload_bytes(length, t.n_off);
     if (e != cudaSuccess) {
         last_cuda_error(e);
         blaze_query_free(q);
@@ -247,6 +264,12 @@ extern "C" int blaze_search_free(blaze_search *s) {
     s->seg_idx.release();
     s->sel_q.release();
     s->seg_keys.release();
+    s->qt_res.release();
+    s->qt_cs.release();
+    s->qt_pack.release();
+    s->qt_pres.release();
+    s->qt_off.release();
+    if (s->h_stage) cudaFreeHost(s->h_stage);
     s->tb_items.release();
     s->tb_out.release();
     s->tb_dirs.release();
@@ -972,15 +995,61 @@ extern "C" int blaze_search_init_hits(blaze_search *s, blaze_init_hit *out, uint
     return k == n_init ? BLAZE_OK : BLAZE_ERR_INTERNAL;
 }
 
+// One call with host buffers: the query's tables go into buffers the search
+// context keeps (grown on demand), copied from pinned staging on the
+// search's stream ahead of the kernels -- no allocation and no device-wide
+// synchronisation per query once warm.
 extern "C" int blaze_prelim_search(blaze_search *s, const uint8_t *query, int32_t length,
                                    const blaze_params *p, blaze_hsp *out, uint64_t capacity,
                                    uint64_t *n_hsps) {
-    if (!s || !p) return BLAZE_ERR_INVALID_ARG;
-    blaze_query *q = nullptr;
-    int rc = blaze_query_create(s->db, query, length, p->word_threshold, &q);
+    if (!s || !p || !query || length <= 0) return BLAZE_ERR_INVALID_ARG;
+    if (length > kMaxQueryLength) return BLAZE_ERR_LIMIT;
+    if (!valid_residues(query, static_cast<uint64_t>(length))) return BLAZE_ERR_INVALID_ARG;
+    int rc = check_params(p);
     if (rc != BLAZE_OK) return rc;
-    rc = blaze_search_run(s, q, p, n_hsps);
-    blaze_query_free(q);
+    BLAZE_CUDA_TRY(cudaSetDevice(s->db->device));
+    QueryTables t;
+    if ((rc = query_tables(query, length, p->word_threshold, t)) != BLAZE_OK) return rc;
+    // pinned staging: residues (+ 64 zero bytes), cell_start, packed cells, presence, hit lists
+    const size_t b_q = (static_cast<size_t>(length) + 64 + 15) & ~size_t{15};
+    const size_t b_cs = sizeof(uint32_t) * (kWords + 1), b_pack = sizeof(uint32_t) * kWords;
+    const size_t b_pres = sizeof(uint32_t) * kPresenceWords, b_off = sizeof(uint16_t) * t.n_off;
+    const size_t o_cs = b_q, o_pack = (o_cs + b_cs + 15) & ~size_t{15}, o_pres = o_pack + b_pack,
+                 o_off = (o_pres + b_pres + 15) & ~size_t{15};
+    if ((rc = ensure_pinned(s->h_stage, s->h_stage_n, o_off + b_off)) != BLAZE_OK) return rc;
+    unsigned char *h = s->h_stage;
+    std::memcpy(h, query, length);
+    std::memset(h + length, 0, b_q - static_cast<size_t>(length));
+    std::memcpy(h + o_cs, t.cs.data(), b_cs);
+    std::memcpy(h + o_pack, t.pack.data(), b_pack);
+    std::memcpy(h + o_pres, t.pres.data(), b_pres);
+    if (b_off) std::memcpy(h + o_off, t.offs, b_off);
+    if ((rc = s->qt_res.ensure(b_q)) != BLAZE_OK) return rc;
+    if ((rc = s->qt_cs.ensure(kWords + 1)) != BLAZE_OK) return rc;
+    if ((rc = s->qt_pack.ensure(kWords)) != BLAZE_OK) return rc;
+    if ((rc = s->qt_pres.ensure(kPresenceWords)) != BLAZE_OK) return rc;
+    if ((rc = s->qt_off.ensure(std::max<uint32_t>(t.n_off, 1))) != BLAZE_OK) return rc;
+    BLAZE_CUDA_TRY(cudaMemcpyAsync(s->qt_res.p, h, b_q, cudaMemcpyHostToDevice, s->stream));
+    BLAZE_CUDA_TRY(cudaMemcpyAsync(s->qt_cs.p, h + o_cs, b_cs, cudaMemcpyHostToDevice, s->stream));
+    BLAZE_CUDA_TRY(cudaMemcpyAsync(s->qt_pack.p, h + o_pack, b_pack, cudaMemcpyHostToDevice, s->stream));
+    BLAZE_CUDA_TRY(cudaMemcpyAsync(s->qt_pres.p, h + o_pres, b_pres, cudaMemcpyHostToDevice, s->stream));
+    if (b_off) BLAZE_CUDA_TRY(cudaMemcpyAsync(s->qt_off.p, h + o_off, b_off, cudaMemcpyHostToDevice, s->stream));
+    blaze_query q;  // views of the search's buffers; not freed
+    q.device = s->db->device;
+    q.qlen = length;
+    q.threshold = p->word_threshold;
+    q.n_off = t.n_off;
+    q.upload_bytes = query_upload_bytes(length, t.n_off);
+    q.d_q = s->qt_res.p;
+    q.d_cell_start = s->qt_cs.p;
+    q.d_cell_pack = s->qt_pack.p;
+    q.d_presence = s->qt_pres.p;
+    q.d_cell_off = s->qt_off.p;
+    RunSpec r;
+    r.q = &q;
+    r.p = p;
+    rc = run_search(s, r, n_hsps);  // synchronises the stream before it returns
+    s->stats.h2d_bytes += q.upload_bytes;
     if (rc != BLAZE_OK) return rc;
     return blaze_search_results(s, out, capacity, n_hsps);
 }

@@ -110,6 +110,12 @@ struct blaze_search {
     DevBuf<unsigned long long> seg_keys;
     GroupDesc *h_groups = nullptr;  // pinned
     size_t h_groups_n = 0;
+    // query tables of the one-call entry point, reused across calls
+    DevBuf<uint8_t> qt_res;
+    DevBuf<uint32_t> qt_cs, qt_pack, qt_pres;
+    DevBuf<uint16_t> qt_off;
+    unsigned char *h_stage = nullptr;  // pinned staging of those tables
+    size_t h_stage_n = 0;
     std::vector<blaze_batch_hsp> batch_results;
     // traceback stage
     DevBuf<TbItem> tb_items;

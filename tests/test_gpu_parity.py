@@ -116,6 +116,28 @@ def test_one_call_host_buffers_and_small_output():
     db.close()
 
 
+def test_one_call_reuses_its_tables_across_query_lengths():
+    # the one-call entry point keeps its query tables between calls: longer,
+    # shorter and degenerate queries in turn must each equal the regular path
+    rng = np.random.default_rng(4242)
+    seqs = [synth.random_residues(rng, int(L)) for L in synth.lognormal_lengths(rng, 800, 250, 0.82, 30, 3000)]
+    qs = [synth.random_residues(rng, L) for L in (700, 5, 1200, 300, 3, 9000, 50, 1)]
+    for i in range(0, len(seqs), 4):
+        q = qs[i % len(qs)]
+        if len(q) > 40:
+            s0 = int(rng.integers(0, len(q) - 40))
+            seqs[i] = np.concatenate([seqs[i], synth.mutate(rng, q[s0:s0 + 40], 0.6)])
+    res, off = concat(seqs)
+    db = blaze103.SeqSrc(res, off)
+    ps = blaze103.PrelimSearch(db)
+    for q in qs + qs[::-1]:
+        p, _ = params_for(len(q), db.tot_len, db.num_seqs)
+        one = ps.prelim_search(q, p, capacity=1 << 16)
+        assert np.array_equal(ps.run(q, p).hsps, one)
+    ps.close()
+    db.close()
+
+
 def test_invalid_inputs_rejected():
     w = synth.make_workload("plain-small", scale=0.01)
     db = blaze103.SeqSrc(w.residues, w.offsets)
