@@ -139,13 +139,9 @@ static int query_tables(const uint8_t *query, int32_t length, int32_t word_thres
     t.cs.assign(kWords + 1, 0u);
     int rc = build_lookup(query, length, word_threshold, t.cs.data(), &t.offs, &t.n_off);
     if (rc != BLAZE_OK) return rc;
-    t.pack.assign(kWords, 0u);
-    t.pres.assign(kPresenceWords, 0u);
-    for (int w = 0; w < kWords; ++w) {
-        const uint32_t cnt = t.cs[w + 1] - t.cs[w];
-        t.pack[w] = (t.cs[w] << 8) | std::min<uint32_t>(cnt, 255u);
-        if (cnt) t.pres[w >> 5] |= 1u << (w & 31);
-    }
+    t.pack.resize(kWords);
+    t.pres.resize(kPresenceWords);
+    pack_word_cells(t.cs.data(), t.pack.data(), t.pres.data());
     return BLAZE_OK;
 }
 

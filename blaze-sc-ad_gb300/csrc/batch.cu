@@ -50,13 +50,8 @@ static int batch_fill(blaze_batch *b, const uint8_t *residues, const uint64_t *o
         b->off_off.push_back(offs_all.size());
         offs_all.insert(offs_all.end(), offs, offs + n_off);
         std::free(offs);
-        uint32_t *pk = pack_all.data() + static_cast<size_t>(i) * kWords;
-        uint32_t *pr = pres_all.data() + static_cast<size_t>(i) * kPresenceWords;
-        for (int w = 0; w < kWords; ++w) {
-            const uint32_t cnt = cs[w + 1] - cs[w];
-            pk[w] = (cs[w] << 8) | std::min<uint32_t>(cnt, 255u);
-            if (cnt) pr[w >> 5] |= 1u << (w & 31);
-        }
+        pack_word_cells(cs, pack_all.data() + static_cast<size_t>(i) * kWords,
+                        pres_all.data() + static_cast<size_t>(i) * kPresenceWords);
     }
     res.resize(res.size() + 64, 0);
     if (offs_all.empty()) offs_all.push_back(0);

@@ -233,6 +233,10 @@ extern const int32_t kBlosum62[kAlphabet][kAlphabet];
 // Word lookup of a query: cell_start[kWords + 1], offsets ascending per cell.
 int build_lookup(const uint8_t *query, int32_t qlen, int32_t threshold,
                  uint32_t *cell_start, uint16_t **offsets, uint32_t *n_offsets);
+// The scan kernel's per-word tables from cell_start: packed cells
+// (start << 8 | min(count, 255); 255 sends the kernel to cell_start) and the
+// word-presence bitset (kPresenceWords words, overwritten).
+void pack_word_cells(const uint32_t *cell_start, uint32_t *pack, uint32_t *presence);
 int default_params(int32_t qlen, uint64_t db_len, uint32_t db_n, double evalue,
                    blaze_params *out);
 

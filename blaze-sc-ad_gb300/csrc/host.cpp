@@ -103,6 +103,15 @@ int build_lookup(const uint8_t *query, int32_t qlen, int32_t threshold, uint32_t
     return BLAZE_OK;
 }
 
+void pack_word_cells(const uint32_t *cell_start, uint32_t *pack, uint32_t *presence) {
+    std::memset(presence, 0, sizeof(uint32_t) * kPresenceWords);
+    for (int w = 0; w < kWords; ++w) {
+        const uint32_t cnt = cell_start[w + 1] - cell_start[w];
+        pack[w] = (cell_start[w] << 8) | std::min<uint32_t>(cnt, 255u);
+        if (cnt) presence[w >> 5] |= 1u << (w & 31);
+    }
+}
+
 // Karlin-Altschul constants of BLOSUM62 (published NCBI table values).
 namespace ka {
 constexpr double kUngappedLambda = 0.3176, kUngappedK = 0.134;
