@@ -18,6 +18,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -97,15 +98,32 @@ int parse_index(const std::string &base, Volume &v) {
     c.pos += (static_cast<size_t>(v.n) + 1) * 4;  // header offsets (.phr): not needed here
     v.seq_off.resize(static_cast<size_t>(v.n) + 1);
     for (auto &o : v.seq_off) o = c.be32();
-    for (uint32_t i = 0; i < v.n; ++i)
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < v.n; ++i) {
         if (v.seq_off[i + 1] <= v.seq_off[i]) return BLAZE_ERR_INVALID_ARG;  // each holds its 0 separator
+        total += v.seq_off[i + 1] - v.seq_off[i] - 1;
+    }
+    if (total != v.total) return BLAZE_ERR_INVALID_ARG;  // the header disagrees with the offsets
     return BLAZE_OK;
+}
+
+// Size of a file in bytes, or -1.
+long long file_size(const std::string &path) {
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) return -1;
+    long long n = -1;
+    if (std::fseek(f, 0, SEEK_END) == 0) n = static_cast<long long>(std::ftell(f));
+    std::fclose(f);
+    return n;
 }
 
 }  // namespace
 
+// Entry points of this file return BLAZE_ERR_OUT_OF_MEMORY where a host
+// allocation fails; no exception crosses the C ABI.
+
 extern "C" int blaze_volume_info(const char *path, uint32_t *n_subjects, uint64_t *total_residues,
-                                 uint32_t *max_length) {
+                                 uint32_t *max_length) try {
     if (!path) return BLAZE_ERR_INVALID_ARG;
     Volume v;
     const int rc = parse_index(path, v);
@@ -114,19 +132,19 @@ extern "C" int blaze_volume_info(const char *path, uint32_t *n_subjects, uint64_
     if (total_residues) *total_residues = v.total;
     if (max_length) *max_length = v.max_len;
     return BLAZE_OK;
+} catch (const std::bad_alloc &) {
+    return BLAZE_ERR_OUT_OF_MEMORY;
 }
 
-extern "C" int blaze_volume_read(const char *path, uint8_t *residues, uint64_t capacity, uint64_t *offsets) {
+extern "C" int blaze_volume_read(const char *path, uint8_t *residues, uint64_t capacity, uint64_t *offsets) try {
     if (!path || !offsets) return BLAZE_ERR_INVALID_ARG;
     Volume v;
     int rc = parse_index(path, v);
     if (rc != BLAZE_OK) return rc;
     std::vector<uint8_t> psq;
     if (!read_file(std::string(path) + ".psq", psq)) return BLAZE_ERR_INVALID_ARG;
-    if (v.n && v.seq_off[v.n] > psq.size()) return BLAZE_ERR_INVALID_ARG;
-    uint64_t total = 0;
-    for (uint32_t i = 0; i < v.n; ++i) total += v.seq_off[i + 1] - v.seq_off[i] - 1;
-    if (total != v.total) return BLAZE_ERR_INVALID_ARG;  // index and sequence file disagree
+    if (v.n && v.seq_off[v.n] > psq.size()) return BLAZE_ERR_INVALID_ARG;  // shorter than the index says
+    const uint64_t total = v.total;
     if (capacity < total) return BLAZE_ERR_OUTPUT_TOO_SMALL;
     if (total && !residues) return BLAZE_ERR_INVALID_ARG;
     uint64_t at = 0;
@@ -138,18 +156,26 @@ extern "C" int blaze_volume_read(const char *path, uint8_t *residues, uint64_t c
         offsets[i + 1] = at;
     }
     return BLAZE_OK;
+} catch (const std::bad_alloc &) {
+    return BLAZE_ERR_OUT_OF_MEMORY;
 }
 
-extern "C" int blaze_db_open(int device, const char *path, blaze_db **out) {
+extern "C" int blaze_db_open(int device, const char *path, blaze_db **out) try {
     if (!out) return BLAZE_ERR_INVALID_ARG;
     *out = nullptr;
     uint32_t n = 0, max_len = 0;
     uint64_t total = 0;
     int rc = blaze_volume_info(path, &n, &total, &max_len);
     if (rc != BLAZE_OK) return rc;
+    // the host copies below are sized by the index: the sequence file must
+    // hold what it claims (a residue and a separator per subject, at least)
+    const long long psq_bytes = file_size(std::string(path) + ".psq");
+    if (psq_bytes < 0 || total + n > static_cast<unsigned long long>(psq_bytes)) return BLAZE_ERR_INVALID_ARG;
     std::vector<uint8_t> res(std::max<uint64_t>(total, 1));
     std::vector<uint64_t> off(static_cast<size_t>(n) + 1);
     rc = blaze_volume_read(path, res.data(), total, off.data());
     if (rc != BLAZE_OK) return rc;
     return blaze_db_create(device, res.data(), off.data(), n, out);
+} catch (const std::bad_alloc &) {
+    return BLAZE_ERR_OUT_OF_MEMORY;
 }

@@ -63,6 +63,26 @@ def test_volume_rejects_malformed(tmp_path):
         volume.read_volume(bad)
     with pytest.raises(blaze103.BlazeError):
         volume.volume_info(os.path.join(tmp_path, "missing"))
+    # a header whose total length disagrees with its own offsets (a huge
+    # claim must be refused before anything is sized by it)
+    pos = 12 + struct.unpack(">I", pin[8:12])[0]
+    pos += 4 + struct.unpack(">I", pin[pos:pos + 4])[0] + 4  # past the date and N
+    with open(bad + ".pin", "wb") as f:
+        f.write(pin[:pos] + struct.pack("<Q", 1 << 50) + pin[pos + 8:])
+    with open(bad + ".psq", "wb") as f:
+        f.write(open(path + ".psq", "rb").read())
+    for call in (volume.volume_info, volume.read_volume, blaze103.SeqSrc.open):
+        with pytest.raises(blaze103.BlazeError) as e:
+            call(bad)
+        assert e.value.status == 1
+    # a sequence file too short for the index: refused before any copy
+    with open(bad + ".pin", "wb") as f:
+        f.write(pin)
+    with open(bad + ".psq", "wb") as f:
+        f.write(b"\0")
+    with pytest.raises(blaze103.BlazeError) as e:
+        blaze103.SeqSrc.open(bad)
+    assert e.value.status == 1
 
 
 @pytest.mark.gpu
