@@ -37,7 +37,7 @@ extern "C" int blaze_device_count(int *count) {
 }
 
 extern "C" int blaze_db_create(int device, const uint8_t *residues, const uint64_t *offsets,
-                               uint32_t n_subjects, blaze_db **out) {
+                               uint32_t n_subjects, blaze_db **out) try {
     if (!out || !offsets || (n_subjects > 0 && !residues)) return BLAZE_ERR_INVALID_ARG;
     *out = nullptr;
     int ndev = 0;
@@ -105,7 +105,7 @@ extern "C" int blaze_db_create(int device, const uint8_t *residues, const uint64
     db->h_off.swap(off);
     *out = db;
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_db_free(blaze_db *db) {
     if (!db) return BLAZE_OK;
@@ -151,7 +151,7 @@ static uint64_t query_upload_bytes(int32_t length, uint32_t n_off) {
 }
 
 extern "C" int blaze_query_create(const blaze_db *db, const uint8_t *query, int32_t length,
-                                  int32_t word_threshold, blaze_query **out) {
+                                  int32_t word_threshold, blaze_query **out) try {
     if (!db || !query || !out || length <= 0) return BLAZE_ERR_INVALID_ARG;
     *out = nullptr;
     if (length > kMaxQueryLength) return BLAZE_ERR_LIMIT;
@@ -184,7 +184,7 @@ extern "C" int blaze_query_create(const blaze_db *db, const uint8_t *query, int3
     }
     *out = q;
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_query_free(blaze_query *q) {
     if (!q) return BLAZE_OK;
@@ -198,7 +198,7 @@ extern "C" int blaze_query_free(blaze_query *q) {
     return BLAZE_OK;
 }
 
-extern "C" int blaze_search_create(blaze_db *db, blaze_search **out) {
+extern "C" int blaze_search_create(blaze_db *db, blaze_search **out) try {
     if (!db || !out) return BLAZE_ERR_INVALID_ARG;
     *out = nullptr;
     BLAZE_CUDA_TRY(cudaSetDevice(db->device));
@@ -229,7 +229,7 @@ extern "C" int blaze_search_create(blaze_db *db, blaze_search **out) {
     if (const char *v = std::getenv("BLAZE_INITIAL_TRACEBACK_CAP")) s->tb_dir_cap = std::max(64, std::atoi(v));
     *out = s;
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_search_free(blaze_search *s) {
     if (!s) return BLAZE_OK;
@@ -875,7 +875,7 @@ static int run_search(blaze_search *s, const RunSpec &spec, uint64_t *n_hsps) {
 }
 
 extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const blaze_params *p,
-                                uint64_t *n_hsps) {
+                                uint64_t *n_hsps) try {
     if (!s || !q || q->device != s->db->device) return BLAZE_ERR_INVALID_ARG;
     int rc = check_params(p);
     if (rc != BLAZE_OK) return rc;
@@ -887,10 +887,10 @@ extern "C" int blaze_search_run(blaze_search *s, const blaze_query *q, const bla
     rc = run_search(s, r, n_hsps);
     s->stats.h2d_bytes += q->upload_bytes;
     return rc;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_search_run_batch(blaze_search *s, const blaze_batch *b, const blaze_params *params,
-                                      uint64_t *n_hsps) {
+                                      uint64_t *n_hsps) try {
     if (!s || !b || !params || b->device != s->db->device || b->n == 0) return BLAZE_ERR_INVALID_ARG;
     for (uint32_t i = 0; i < b->n; ++i) {
         int rc = check_params(&params[i]);
@@ -907,10 +907,10 @@ extern "C" int blaze_search_run_batch(blaze_search *s, const blaze_batch *b, con
     int rc = run_search(s, r, n_hsps);
     s->stats.h2d_bytes += b->upload_bytes;
     return rc;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_search_batch_results(const blaze_search *s, blaze_batch_hsp *out, uint64_t capacity,
-                                          uint64_t *n_hsps) {
+                                          uint64_t *n_hsps) try {
     if (!s) return BLAZE_ERR_INVALID_ARG;
     if (n_hsps) *n_hsps = s->batch_results.size();
     if (capacity < s->batch_results.size()) return BLAZE_ERR_OUTPUT_TOO_SMALL;
@@ -919,9 +919,9 @@ extern "C" int blaze_search_batch_results(const blaze_search *s, blaze_batch_hsp
         std::memcpy(out, s->batch_results.data(), sizeof(blaze_batch_hsp) * s->batch_results.size());
     }
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
-extern "C" int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t) {
+extern "C" int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t) try {
     if (!s || !t) return BLAZE_ERR_INVALID_ARG;
     if (t->stage_bytes > 16384 || t->max_warps_per_block > static_cast<uint32_t>(kScanMaxWarpsPerBlock))
         return BLAZE_ERR_LIMIT;
@@ -931,10 +931,10 @@ extern "C" int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t) {
     s->tile_residues = t->tile_residues;
     s->max_warps = t->max_warps_per_block;
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_search_results(const blaze_search *s, blaze_hsp *out, uint64_t capacity,
-                                    uint64_t *n_hsps) {
+                                    uint64_t *n_hsps) try {
     if (!s) return BLAZE_ERR_INVALID_ARG;
     if (n_hsps) *n_hsps = s->results.size();
     if (capacity < s->results.size()) return BLAZE_ERR_OUTPUT_TOO_SMALL;
@@ -943,7 +943,7 @@ extern "C" int blaze_search_results(const blaze_search *s, blaze_hsp *out, uint6
         std::memcpy(out, s->results.data(), sizeof(blaze_hsp) * s->results.size());
     }
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_search_stats(const blaze_search *s, blaze_stats *out) {
     if (!s || !out) return BLAZE_ERR_INVALID_ARG;
@@ -952,7 +952,7 @@ extern "C" int blaze_search_stats(const blaze_search *s, blaze_stats *out) {
 }
 
 extern "C" int blaze_search_init_hits(blaze_search *s, blaze_init_hit *out, uint64_t capacity,
-                                      uint64_t *n_hits) {
+                                      uint64_t *n_hits) try {
     if (!s || s->last_batched) return BLAZE_ERR_INVALID_ARG;  // single-query runs only
     const size_t n_init = static_cast<size_t>(s->last_init_count);
     const size_t n_work = static_cast<size_t>(s->last_work_count);
@@ -989,7 +989,7 @@ extern "C" int blaze_search_init_hits(blaze_search *s, blaze_init_hit *out, uint
     }
     if (n_hits) *n_hits = k;
     return k == n_init ? BLAZE_OK : BLAZE_ERR_INTERNAL;
-}
+} BLAZE_ABI_CATCH
 
 // One call with host buffers: the query's tables go into buffers the search
 // context keeps (grown on demand), copied from pinned staging on the
@@ -997,7 +997,7 @@ extern "C" int blaze_search_init_hits(blaze_search *s, blaze_init_hit *out, uint
 // synchronisation per query once warm.
 extern "C" int blaze_prelim_search(blaze_search *s, const uint8_t *query, int32_t length,
                                    const blaze_params *p, blaze_hsp *out, uint64_t capacity,
-                                   uint64_t *n_hsps) {
+                                   uint64_t *n_hsps) try {
     if (!s || !p || !query || length <= 0) return BLAZE_ERR_INVALID_ARG;
     if (length > kMaxQueryLength) return BLAZE_ERR_LIMIT;
     if (!valid_residues(query, static_cast<uint64_t>(length))) return BLAZE_ERR_INVALID_ARG;
@@ -1048,4 +1048,4 @@ extern "C" int blaze_prelim_search(blaze_search *s, const uint8_t *query, int32_
     s->stats.h2d_bytes += q.upload_bytes;
     if (rc != BLAZE_OK) return rc;
     return blaze_search_results(s, out, capacity, n_hsps);
-}
+} BLAZE_ABI_CATCH

@@ -94,7 +94,7 @@ static int batch_fill(blaze_batch *b, const uint8_t *residues, const uint64_t *o
 }
 
 extern "C" int blaze_batch_create(const blaze_db *db, const uint8_t *residues, const uint64_t *offsets,
-                                  uint32_t n_queries, int32_t word_threshold, blaze_batch **out) {
+                                  uint32_t n_queries, int32_t word_threshold, blaze_batch **out) try {
     if (!db || !out) return BLAZE_ERR_INVALID_ARG;
     *out = nullptr;
     const int vrc = check_batch_input(residues, offsets, n_queries);
@@ -109,7 +109,7 @@ extern "C" int blaze_batch_create(const blaze_db *db, const uint8_t *residues, c
     }
     *out = b;
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
 int batch_refill(blaze_search *s, blaze_batch **inout, const uint8_t *residues, const uint64_t *offsets,
                  uint32_t n_queries, int32_t word_threshold) {

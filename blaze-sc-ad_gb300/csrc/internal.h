@@ -2,6 +2,7 @@
 // not part of the C ABI.
 #pragma once
 #include <cstdint>
+#include <new>
 
 #include "blaze_prelim.h"
 
@@ -15,3 +16,13 @@ int batch_refill(blaze_search *s, blaze_batch **batch, const uint8_t *residues, 
 // worker thread's error can be handed to the thread that reads the status.
 int last_cuda_error_code();
 void set_last_cuda_error_code(int code);
+
+// Handler of a function-try-block around a C entry point: no C++ exception
+// (a failed host allocation or thread start) crosses the C ABI.
+#define BLAZE_ABI_CATCH                                \
+    catch (const std::bad_alloc &) {                   \
+        return BLAZE_ERR_OUT_OF_MEMORY;                \
+    }                                                  \
+    catch (...) {                                      \
+        return BLAZE_ERR_INTERNAL;                     \
+    }

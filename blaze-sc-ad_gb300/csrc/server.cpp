@@ -24,6 +24,7 @@ using Clock = std::chrono::steady_clock;
 constexpr uint64_t kPerQueryFixed = 1u << 20;
 constexpr uint64_t kPerResidue = 512;
 constexpr uint64_t kTableBytes = 4ull * (2 * 21952 + 1 + 686);
+constexpr uint32_t kMaxSlots = 64;  // worker threads (each with its search context)
 
 struct Request {
     uint64_t ticket;
@@ -124,24 +125,28 @@ void worker(blaze_server *s) {
     uint64_t bytes = 0;
     while (take_batch(s, batch, bytes)) {
         const size_t n = batch.size();
-        std::vector<uint8_t> res;
-        std::vector<uint64_t> off(n + 1, 0);
-        std::vector<blaze_params> params(n);
         uint64_t batch_residues = 0;
-        for (size_t i = 0; i < n; ++i) {
-            res.insert(res.end(), batch[i].residues.begin(), batch[i].residues.end());
-            off[i + 1] = res.size();
-            blaze_params_default(static_cast<int32_t>(batch[i].residues.size()), s->db_residues, s->db_subjects,
-                                 s->cfg.evalue, &params[i]);
-            batch_residues += s->db_residues;
-        }
         int rc = create_rc;
         uint64_t n_hsps = 0;
-        if (rc == BLAZE_OK) rc = batch_refill(search, &b, res.data(), off.data(), static_cast<uint32_t>(n), 11);
-        if (rc == BLAZE_OK) rc = blaze_search_run_batch(search, b, params.data(), &n_hsps);
-        if (rc == BLAZE_OK) {
-            out.resize(n_hsps);
-            rc = blaze_search_batch_results(search, out.data(), n_hsps, &n_hsps);
+        try {  // a failed host allocation fails this batch, not the process
+            std::vector<uint8_t> res;
+            std::vector<uint64_t> off(n + 1, 0);
+            std::vector<blaze_params> params(n);
+            for (size_t i = 0; i < n; ++i) {
+                res.insert(res.end(), batch[i].residues.begin(), batch[i].residues.end());
+                off[i + 1] = res.size();
+                blaze_params_default(static_cast<int32_t>(batch[i].residues.size()), s->db_residues,
+                                     s->db_subjects, s->cfg.evalue, &params[i]);
+                batch_residues += s->db_residues;
+            }
+            if (rc == BLAZE_OK) rc = batch_refill(search, &b, res.data(), off.data(), static_cast<uint32_t>(n), 11);
+            if (rc == BLAZE_OK) rc = blaze_search_run_batch(search, b, params.data(), &n_hsps);
+            if (rc == BLAZE_OK) {
+                out.resize(n_hsps);
+                rc = blaze_search_batch_results(search, out.data(), n_hsps, &n_hsps);
+            }
+        } catch (const std::bad_alloc &) {
+            rc = BLAZE_ERR_OUT_OF_MEMORY;
         }
         const auto now = Clock::now();
         const int cuda_error = rc == BLAZE_ERR_CUDA ? last_cuda_error_code() : 0;
@@ -182,20 +187,32 @@ double percentile(std::vector<double> v, double p) {
 
 }  // namespace
 
-extern "C" int blaze_server_create(blaze_db *db, const blaze_server_config *cfg, blaze_server **out) {
+extern "C" int blaze_server_create(blaze_db *db, const blaze_server_config *cfg, blaze_server **out) try {
     if (!db || !cfg || !out || cfg->slots == 0 || cfg->max_batch == 0 || cfg->evalue <= 0) return BLAZE_ERR_INVALID_ARG;
     *out = nullptr;
+    if (cfg->slots > kMaxSlots) return BLAZE_ERR_LIMIT;
     auto *s = new blaze_server();
     s->db = db;
     s->cfg = *cfg;
     uint32_t max_len = 0;
     blaze_db_info(db, &s->db_residues, &s->db_subjects, &max_len);
-    for (uint32_t i = 0; i < cfg->slots; ++i) s->workers.emplace_back(worker, s);
+    try {
+        for (uint32_t i = 0; i < cfg->slots; ++i) s->workers.emplace_back(worker, s);
+    } catch (...) {  // a thread that would not start: stop the ones that did
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stopping = true;
+        }
+        s->queue_cv.notify_all();
+        for (std::thread &t : s->workers) t.join();
+        delete s;
+        return BLAZE_ERR_INTERNAL;
+    }
     *out = s;
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
-extern "C" int blaze_server_submit(blaze_server *s, const uint8_t *query, int32_t length, uint64_t *ticket) {
+extern "C" int blaze_server_submit(blaze_server *s, const uint8_t *query, int32_t length, uint64_t *ticket) try {
     if (!s || !query || length <= 0 || !ticket) return BLAZE_ERR_INVALID_ARG;
     if (length > 32000) return BLAZE_ERR_LIMIT;
     for (int32_t i = 0; i < length; ++i)
@@ -219,9 +236,9 @@ extern "C" int blaze_server_submit(blaze_server *s, const uint8_t *query, int32_
     }
     s->queue_cv.notify_one();
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
-extern "C" int blaze_server_wait(blaze_server *s, uint64_t ticket, int32_t timeout_ms, uint64_t *n_hsps) {
+extern "C" int blaze_server_wait(blaze_server *s, uint64_t ticket, int32_t timeout_ms, uint64_t *n_hsps) try {
     if (!s) return BLAZE_ERR_INVALID_ARG;
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->results.find(ticket);
@@ -236,10 +253,10 @@ extern "C" int blaze_server_wait(blaze_server *s, uint64_t ticket, int32_t timeo
     if (n_hsps) *n_hsps = r.hsps.size();
     if (r.status == BLAZE_ERR_CUDA) set_last_cuda_error_code(r.cuda_error);
     return r.status;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_server_take(blaze_server *s, uint64_t ticket, blaze_hsp *out, uint64_t capacity,
-                                 uint64_t *n_hsps, double *latency_ms) {
+                                 uint64_t *n_hsps, double *latency_ms) try {
     if (!s) return BLAZE_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->results.find(ticket);
@@ -260,9 +277,9 @@ extern "C" int blaze_server_take(blaze_server *s, uint64_t ticket, blaze_hsp *ou
     }
     s->results.erase(it);
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
-extern "C" int blaze_server_stats_get(blaze_server *s, blaze_server_stats *out) {
+extern "C" int blaze_server_stats_get(blaze_server *s, blaze_server_stats *out) try {
     if (!s || !out) return BLAZE_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(s->mu);
     std::memset(out, 0, sizeof(*out));
@@ -276,7 +293,7 @@ extern "C" int blaze_server_stats_get(blaze_server *s, blaze_server_stats *out) 
     if (s->any_submit && s->completed)
         out->busy_s = std::chrono::duration<double>(s->last_done - s->first_submit).count();
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_server_free(blaze_server *s) {
     if (!s) return BLAZE_OK;

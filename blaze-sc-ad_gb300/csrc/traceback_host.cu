@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "handles.h"
+#include "internal.h"
 
 // ------------------------------------------------------------------------
 // Traceback stage.
@@ -163,7 +164,7 @@ static int tb_item(const blaze_db *db, const blaze_hsp &h, int32_t qlen, uint32_
 }
 
 extern "C" int blaze_search_traceback(blaze_search *s, const blaze_query *q, const blaze_params *p,
-                                      int32_t final_xdrop, double evalue, uint64_t *n_hsps) {
+                                      int32_t final_xdrop, double evalue, uint64_t *n_hsps) try {
     if (!s || !q || !p || final_xdrop <= 0 || q->device != s->db->device || s->last_batched)
         return BLAZE_ERR_INVALID_ARG;
     int rc = check_params(p);
@@ -188,10 +189,10 @@ extern "C" int blaze_search_traceback(blaze_search *s, const blaze_query *q, con
     }
     if (n_hsps) *n_hsps = s->tb_results.size();
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_search_traceback_batch(blaze_search *s, const blaze_batch *b, const blaze_params *params,
-                                            int32_t final_xdrop, double evalue, uint64_t *n_hsps) {
+                                            int32_t final_xdrop, double evalue, uint64_t *n_hsps) try {
     if (!s || !b || !params || final_xdrop <= 0 || !s->last_batched || s->last_batch != b)
         return BLAZE_ERR_INVALID_ARG;
     int rc;
@@ -228,7 +229,7 @@ extern "C" int blaze_search_traceback_batch(blaze_search *s, const blaze_batch *
     }
     if (n_hsps) *n_hsps = s->tb_batch_results.size();
     return BLAZE_OK;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_search_traceback_batch_results(const blaze_search *s, blaze_batch_aligned_hsp *out,
                                                     uint64_t capacity, uint64_t *n_hsps) {

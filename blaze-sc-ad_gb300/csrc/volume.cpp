@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "blaze_prelim.h"
+#include "internal.h"
 
 namespace {
 
@@ -119,9 +120,6 @@ long long file_size(const std::string &path) {
 
 }  // namespace
 
-// Entry points of this file return BLAZE_ERR_OUT_OF_MEMORY where a host
-// allocation fails; no exception crosses the C ABI.
-
 extern "C" int blaze_volume_info(const char *path, uint32_t *n_subjects, uint64_t *total_residues,
                                  uint32_t *max_length) try {
     if (!path) return BLAZE_ERR_INVALID_ARG;
@@ -132,9 +130,7 @@ extern "C" int blaze_volume_info(const char *path, uint32_t *n_subjects, uint64_
     if (total_residues) *total_residues = v.total;
     if (max_length) *max_length = v.max_len;
     return BLAZE_OK;
-} catch (const std::bad_alloc &) {
-    return BLAZE_ERR_OUT_OF_MEMORY;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_volume_read(const char *path, uint8_t *residues, uint64_t capacity, uint64_t *offsets) try {
     if (!path || !offsets) return BLAZE_ERR_INVALID_ARG;
@@ -156,9 +152,7 @@ extern "C" int blaze_volume_read(const char *path, uint8_t *residues, uint64_t c
         offsets[i + 1] = at;
     }
     return BLAZE_OK;
-} catch (const std::bad_alloc &) {
-    return BLAZE_ERR_OUT_OF_MEMORY;
-}
+} BLAZE_ABI_CATCH
 
 extern "C" int blaze_db_open(int device, const char *path, blaze_db **out) try {
     if (!out) return BLAZE_ERR_INVALID_ARG;
@@ -176,6 +170,4 @@ extern "C" int blaze_db_open(int device, const char *path, blaze_db **out) try {
     rc = blaze_volume_read(path, res.data(), total, off.data());
     if (rc != BLAZE_OK) return rc;
     return blaze_db_create(device, res.data(), off.data(), n, out);
-} catch (const std::bad_alloc &) {
-    return BLAZE_ERR_OUT_OF_MEMORY;
-}
+} BLAZE_ABI_CATCH

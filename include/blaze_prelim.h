@@ -4,7 +4,8 @@
  * ungapped X-drop -> semi-gapped X-drop -> per-subject HSP lists).
  *
  * Plain pointers and sizes only. Every entry point returns a blaze_status
- * (0 = success) and never exits the process. Handles are not thread-safe;
+ * (0 = success), never exits the process and lets no C++ exception out (a
+ * failed host allocation is BLAZE_ERR_OUT_OF_MEMORY). Handles are not thread-safe;
  * use one blaze_search per host thread (each owns its CUDA stream).
  *
  * Reference interfaces replaced (paths within 181charan/BLAZE-SC-ad):
@@ -285,7 +286,7 @@ int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t);
 typedef struct blaze_server blaze_server;
 
 typedef struct blaze_server_config {
-    uint32_t slots;           /* batches in flight at once (>= 1) */
+    uint32_t slots;           /* batches in flight at once (1..64; BLAZE_ERR_LIMIT above) */
     uint32_t max_batch;       /* queries per batch at most (>= 1) */
     uint64_t memory_budget;   /* bytes for in-flight batches (0: no limit) */
     uint32_t batch_window_us; /* after the first waiting query, wait this long for more */

@@ -104,6 +104,9 @@ def test_server_rejects_bad_input(served):
     with pytest.raises(blaze103.BlazeError):  # a ticket is released once taken
         srv.wait(t)
     srv.close()
+    with pytest.raises(blaze103.BlazeError) as e:  # more worker threads than the library runs
+        blaze103.Server(db, slots=65)
+    assert e.value.status == 6  # BLAZE_ERR_LIMIT
 
 
 def test_concurrent_search_contexts(served):
