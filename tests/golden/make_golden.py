@@ -1,6 +1,6 @@
 """Regenerate the oracle regression fixtures in this directory.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture name ...]
 
 Each fixture holds a seeded synthetic case (query, residues, offsets), the
 search parameters, the oracle's init hits and final HSPs for it, and the
@@ -43,10 +43,33 @@ def cases():
     off = np.zeros(len(seqs) + 1, dtype=np.uint64)
     off[1:] = np.cumsum([len(s) for s in seqs])
     yield "lowcomplexity_homologs", q, np.concatenate(seqs), off, (50_000_000, 150_000)
+    # the overflow-stress shape, small: a 2,257-residue query, 80 subjects
+    # with low-complexity runs and 30-60 % homologs, plus two long subjects
+    # (12,000 and 33,000 residues) holding homologs and a low-complexity run
+    w = synth.make_workload("overflow-stress", scale=0.00016)
+    q = w.queries[1]
+    rng = np.random.default_rng(33)
+    seqs = [w.residues[int(w.offsets[i]):int(w.offsets[i + 1])] for i in range(w.n_subjects)]
+    for L in (12_000, 33_000):
+        s = synth.random_residues(rng, L)
+        for _ in range(3):
+            s0 = int(rng.integers(0, len(q) - 300))
+            hom = synth.mutate(rng, q[s0:s0 + 300], float(rng.uniform(0.3, 0.6)))
+            p = int(rng.integers(0, len(s) - len(hom)))
+            s[p:p + len(hom)] = hom
+        run = alpha[rng.integers(0, 3, 150)]
+        p = int(rng.integers(0, len(s) - 150))
+        s[p:p + 150] = run
+        seqs.append(s)
+    off = np.zeros(len(seqs) + 1, dtype=np.uint64)
+    off[1:] = np.cumsum([len(s) for s in seqs])
+    yield "overflow_stress_small", q, np.concatenate(seqs), off, (60_000_000, 100_000)
 
 
-def main():
+def main(only=()):
     for name, q, res, off, (dblen, dbn) in cases():
+        if only and name not in only:
+            continue
         p = oracle.default_params(len(q), dblen, dbn)
         hsps, inits = oracle.search_db(q, res, off, p, threads=4, want_inits=True)
         traced = traced_records(q, res, off, hsps, p)
@@ -74,4 +97,4 @@ def traced_records(q, res, off, hsps, p):
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))  # fixture names to regenerate (default: all)
