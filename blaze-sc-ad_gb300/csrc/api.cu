@@ -509,6 +509,7 @@ static int run_pass(blaze_search *s, const RunSpec &r, const std::vector<ScanPla
         sa.stage_bytes = lay.stage_bytes;
         sa.query_smem_bytes = lay.query_smem_bytes;
         sa.warp_smem_bytes = lay.warp_smem_bytes;
+        sa.smem_bytes = static_cast<uint32_t>(lay.smem_bytes);
         sa.scratch = s->scratch.p;
         sa.scratch_cap = s->scratch_cap;
         sa.init_out = s->init_out.p;
@@ -619,14 +620,38 @@ static int run_search(blaze_search *s, const RunSpec &spec, uint64_t *n_hsps) {
                                            scan_batch_max_warps_by_registers(false))
                                 : scan_max_warps_by_registers(r.q->qlen <= static_cast<int32_t>(kQuerySmemMax));
     const int warp_cap = s->max_warps ? std::min(reg_cap, static_cast<int>(s->max_warps)) : reg_cap;
-    // layout of one scan launch for queries up to max_qlen
+    // layout of one single-query scan launch
     auto layout_for = [&](int32_t max_qlen) {
         return scan_layout(max_qlen, p0->window, s->stage_bytes, kSmemBudget, warp_cap);
     };
-    // Length classes: a launch sizes every warp's diagonal table for its
-    // longest query, so a batch is split, shortest first, into classes whose
-    // longest query still leaves at least 4/5 of the warps per block that its
-    // shortest would get; each class is one scan launch.
+    // layout of one batched scan launch over queries of up to `longest`
+    // residues: shared memory for all the block's warps at the longest query
+    // when that fits the budget, else the whole budget (at least one warp);
+    // each tile runs as many warps as fit for its own query
+    auto batch_layout_for = [&](int32_t longest) {
+        ScanLayout l{};
+        const uint32_t stage_region = (s->stage_bytes + 32u + 15u) & ~15u;
+        auto warp_bytes = [&](int32_t qlen) {
+            const uint32_t e = static_cast<uint32_t>(qlen + p0->window + 3) & ~3u;
+            return static_cast<size_t>(((4u * e + 15u) & ~15u) + 2u * kDeferCap * sizeof(uint2) +
+                                       kSeedCap * sizeof(int4) + stage_region);
+        };
+        const int w = std::max(1, std::min(warp_cap, kScanMaxWarpsPerBlock));
+        l.query_smem_bytes = longest <= kQuerySmemMax ? (static_cast<uint32_t>(longest) + 15u) & ~15u : 0u;
+        const size_t regions = kScanMatBytes + kScanPresenceBytes + l.query_smem_bytes + 16u * static_cast<size_t>(w);
+        l.smem_bytes = std::max(std::min(kSmemBudget, regions + static_cast<size_t>(w) * warp_bytes(longest)),
+                                regions + warp_bytes(longest));
+        l.warps_per_block = w;
+        l.stage_bytes = s->stage_bytes;
+        l.diag_entries = static_cast<uint32_t>(longest + p0->window + 3) & ~3u;
+        l.diag_magic = static_cast<uint32_t>((1ull << 32) / l.diag_entries + 1);
+        l.diag_bytes = 4u * l.diag_entries;
+        l.warp_smem_bytes = static_cast<uint32_t>(warp_bytes(longest));
+        return l;
+    };
+    // Batched: one scan launch for the queries whose residues fit the
+    // block's shared-memory copy and one for any longer ones (their tiles
+    // size the warps' tables per query).
     std::vector<uint32_t> order(nq);
     std::iota(order.begin(), order.end(), 0u);
     if (batched)
@@ -634,15 +659,29 @@ static int run_search(blaze_search *s, const RunSpec &spec, uint64_t *n_hsps) {
                          [&](uint32_t a, uint32_t b) { return r.b->qlen[a] < r.b->qlen[b]; });
     auto qlen_at = [&](uint32_t k) { return batched ? r.b->qlen[order[k]] : r.q->qlen; };
     std::vector<ScanPlan> plans;
+    // A launch's shared memory fixes the SM's L1 share for all of it, and the
+    // L1 keeps the word tables the finder reads per position; so batched
+    // queries are grouped by the shared-memory step (of the SM's carve-out
+    // choices) that all the block's warps need for them, each group one launch
+    // sized for its longest query -- what a single-query launch does per query.
+    auto smem_step = [&](int32_t qlen) {
+        constexpr size_t kSteps[] = {100u << 10, 132u << 10, 164u << 10, 196u << 10};
+        const size_t need = batch_layout_for(qlen).smem_bytes;
+        int k = 0;
+        while (k < 4 && need > kSteps[k]) ++k;
+        return k + (qlen > kQuerySmemMax ? 8 : 0);  // longer queries stay in global memory: own launch
+    };
     for (uint32_t i = 0; i < nq;) {
-        const int base_w = layout_for(qlen_at(i)).warps_per_block;
         uint32_t j = i + 1;
-        while (j < nq && 5 * layout_for(qlen_at(j)).warps_per_block >= 4 * base_w) ++j;
+        if (batched) {
+            const int step = smem_step(qlen_at(i));
+            while (j < nq && smem_step(qlen_at(j)) == step) ++j;
+        }
         ScanPlan pl;
-        pl.lay = layout_for(qlen_at(j - 1));
+        pl.lay = batched ? batch_layout_for(qlen_at(j - 1)) : layout_for(qlen_at(j - 1));
         pl.first = i;
         pl.n = j - i;
-        if (pl.lay.smem_bytes > 227 * 1024) return BLAZE_ERR_LIMIT;
+        if (pl.lay.smem_bytes > 227 * 1024 - 64) return BLAZE_ERR_LIMIT;  // the opt-in limit less static shared memory
         int per_sm = 0;
         if (batched) {
             BLAZE_CUDA_TRY(scan_batch_occupancy(pl.lay.query_smem_bytes != 0, pl.lay.warps_per_block, pl.lay.smem_bytes,
@@ -656,12 +695,12 @@ static int run_search(blaze_search *s, const RunSpec &spec, uint64_t *n_hsps) {
             if (s->tile_residues) {
                 pl.tile_residues = s->tile_residues;
             } else {
-                // several tiles' worth per warp, at most kMaxTileResidues
-                // each (a block's tile is that times its warps); a power of
-                // two so that few distinct bound tables exist
-                const uint64_t warps = static_cast<uint64_t>(pl.blocks) * pl.lay.warps_per_block;
-                const uint64_t ranges = (4 * warps + pl.n - 1) / pl.n;
-                uint64_t t = std::max<uint64_t>(db->total / std::max<uint64_t>(ranges, 1), 1);
+                // about 16 tiles per block (its warps wait for the last one
+                // at each tile's end, so larger tiles waste less), at most
+                // kMaxTileResidues per warp; a power of two so that few
+                // distinct bound tables exist
+                const uint64_t per_block = db->total * pl.n / (16ull * static_cast<uint64_t>(pl.blocks));
+                uint64_t t = std::max<uint64_t>(per_block / static_cast<uint64_t>(pl.lay.warps_per_block), 1);
                 t = std::min<uint64_t>(t, kMaxTileResidues);
                 uint32_t pow2 = 1;
                 while (static_cast<uint64_t>(pow2) * 2 <= t) pow2 *= 2;

@@ -27,7 +27,7 @@ constexpr size_t kScanMatBytes = kAlphabet * kAlphabet;               // int8 ma
 constexpr size_t kScanPresenceBytes = (kPresenceWords * 4 + 15) & ~15; // 2752
 constexpr int32_t kQuerySmemMax = 8192;      // queries up to this length live in shared memory
 constexpr uint32_t kScanStageBytes = 1024;   // subjects up to this length are staged
-constexpr uint32_t kMaxTileResidues = 1u << 12;  // automatic tile size at most (residues)
+constexpr uint32_t kMaxTileResidues = 1u << 16;  // automatic tile size at most (residues per warp)
 
 // An ungapped HSP that reached the ungapped cutoff (NCBI BlastInitHSP analog).
 struct InitHit {
@@ -111,6 +111,7 @@ struct ScanArgs {
     uint32_t diag_magic;         // floor(2^32 / diag_entries) + 1
     uint32_t diag_bytes, stage_bytes, query_smem_bytes, warp_smem_bytes;
     uint32_t diag_entries_max;   // largest table any query of the launch uses
+    uint32_t smem_bytes;         // batched launches: dynamic shared memory of a block
     // batched launches only
     const BatchQuery *queries;   // n_queries descriptors
     uint32_t n_queries;

@@ -630,7 +630,7 @@ __device__ __forceinline__ void process_subject(Finder &f, const ScanArgs &a, co
     f.base += static_cast<uint32_t>(slen + c.window);
     __syncwarp();
     if (f.base > kBaseReset) {
-        for (uint32_t i = lane; i < a.diag_entries_max; i += 32) sts32(f.diag + 4u * i, 0u);
+        for (uint32_t i = lane; i < c.diag_entries; i += 32) sts32(f.diag + 4u * i, 0u);
         f.base = 0;
         __syncwarp();
     }
@@ -722,20 +722,40 @@ scan_kernel(const ScanArgs a) {
 // subjects come first and queries interleave. Ranges hold about equal
 // residues (host-computed bounds, sized for a whole block). A block stages
 // its tile's query tables in shared memory -- the word-presence bitset and,
-// up to kQuerySmemMax residues, the query -- and its warps take the range's
-// subjects longest first from a shared cursor; the block restages only
-// after every warp has left the tile.
+// up to kQuerySmemMax residues, the query -- and lays its warps' regions out
+// for that query: each warp's diagonal table takes the query's length plus
+// the window, so as many warps as fit (at most the block's) take the range's
+// subjects, longest first, from a shared cursor; the others sit the tile out.
+// The block restages only after every warp has left the tile. Shared memory:
+// matrix, presence bitset, query, one pair of mbarriers per warp, then the
+// warps' regions (diagonal table, deferred hits, seeds, stage buffer).
 template <bool QS>
 __global__ void __launch_bounds__(kScanMaxWarpsPerBlock * 32, 1)
 scan_batch_kernel(const ScanArgs a) {
     __shared__ unsigned long long s_tile;
     __shared__ uint32_t s_next;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t n_warps = blockDim.x >> 5;
     for (int i = threadIdx.x; i < kAlphabet * kAlphabet; i += blockDim.x)
         reinterpret_cast<int8_t *>(smem)[kMatOff + i] = g_blosum8[i];
-    uint32_t stage = 0;
-    Finder f = make_finder(a, a.query_smem_bytes, stage);
+    const uint32_t bars = kQueryOff + a.query_smem_bytes;  // 16-byte aligned
+    const uint32_t regions = bars + 16u * n_warps;
+    Finder f;
+    f.bars = bars + 16u * static_cast<uint32_t>(warp);
+    f.phase = 0u;
+    f.n_defer = f.n_seed = f.sel = 0;
+    f.base = 0;
+    f.extensions = 0;
+    f.n_init = 0;
+    f.scratch = a.scratch + ((static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) *
+                                a.scratch_cap;
+    if (lane == 0) {
+        mbar_init(smem_base() + f.bars);
+        mbar_init(smem_base() + f.bars + 8u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     const unsigned long long n_tiles = static_cast<unsigned long long>(a.n_ranges) * a.n_queries;
+    const uint32_t fixed_warp_bytes = 2u * kDeferCap * sizeof(uint2) + kSeedCap * sizeof(int4) + stage_region(a);
     unsigned long long word_hits = 0, residues = 0;
     bool staging = true;  // false after a bulk copy that never landed (kFlagBadState is set)
     for (;;) {
@@ -753,37 +773,49 @@ scan_batch_kernel(const ScanArgs a) {
         if (QS)
             for (int i = threadIdx.x; i < bq.qlen; i += blockDim.x) smem[kQueryOff + i] = bq.q[i];
         __syncthreads();
-        Ctx c;
-        c.q = bq.q;
-        c.qlen = bq.qlen;
-        c.cell_start = bq.cell_start;
-        c.cell_pack = bq.cell_pack;
-        c.presence = bq.presence;
-        c.cell_off = bq.cell_off;
-        c.diag_entries = bq.diag_entries;
-        c.diag_magic = bq.diag_magic;
-        c.window = a.window;
-        c.xdrop = a.xdrop;
-        c.cutoff = bq.ungapped_cutoff;
-        Query<QS> q;
-        q.ptr = bq.q;
-        q.len = bq.qlen;
-        const uint32_t hi = a.tile_bounds[range], lo = a.tile_bounds[range + 1];
-        for (;;) {
-            uint32_t k = 0;
-            if (lane == 0) k = atomicAdd(&s_next, 1u);
-            k = __shfl_sync(kFull, k, 0);
-            if (k >= hi - lo) break;
-            const uint32_t subj = hi - 1u - k;
-            bool staged = staging && stage_issue(f, a, stage, 0, subj);
-            if (staged && !stage_wait(f, a, 0)) {
-                // the copy never landed: read this and every later subject
-                // from global memory (the host reports the run as failed)
-                staging = false;
-                staged = false;
+        const uint32_t diag_bytes = (4u * bq.diag_entries + 15u) & ~15u;
+        const uint32_t warp_bytes = diag_bytes + fixed_warp_bytes;
+        const uint32_t active = min(n_warps, (a.smem_bytes - regions) / warp_bytes);  // >= 1 (host)
+        if (static_cast<uint32_t>(warp) < active) {
+            f.diag = regions + static_cast<uint32_t>(warp) * warp_bytes;
+            f.defer = f.diag + diag_bytes;
+            f.seeds = f.defer + 2u * kDeferCap * sizeof(uint2);
+            const uint32_t stage = f.seeds + kSeedCap * sizeof(int4);
+            for (uint32_t i = lane; i < bq.diag_entries; i += 32) sts32(f.diag + 4u * i, 0u);
+            f.base = 0;
+            __syncwarp();
+            Ctx c;
+            c.q = bq.q;
+            c.qlen = bq.qlen;
+            c.cell_start = bq.cell_start;
+            c.cell_pack = bq.cell_pack;
+            c.presence = bq.presence;
+            c.cell_off = bq.cell_off;
+            c.diag_entries = bq.diag_entries;
+            c.diag_magic = bq.diag_magic;
+            c.window = a.window;
+            c.xdrop = a.xdrop;
+            c.cutoff = bq.ungapped_cutoff;
+            Query<QS> q;
+            q.ptr = bq.q;
+            q.len = bq.qlen;
+            const uint32_t hi = a.tile_bounds[range], lo = a.tile_bounds[range + 1];
+            for (;;) {
+                uint32_t k = 0;
+                if (lane == 0) k = atomicAdd(&s_next, 1u);
+                k = __shfl_sync(kFull, k, 0);
+                if (k >= hi - lo) break;
+                const uint32_t subj = hi - 1u - k;
+                bool staged = staging && stage_issue(f, a, stage, 0, subj);
+                if (staged && !stage_wait(f, a, 0)) {
+                    // the copy never landed: read this and every later subject
+                    // from global memory (the host reports the run as failed)
+                    staging = false;
+                    staged = false;
+                }
+                process_subject<QS, true>(f, a, c, q, subj, bq.index, staged ? stage : kNoStage, word_hits,
+                                          residues);
             }
-            process_subject<QS, true>(f, a, c, q, subj, bq.index, staged ? stage : kNoStage, word_hits,
-                                      residues);
         }
         __syncthreads();
     }
