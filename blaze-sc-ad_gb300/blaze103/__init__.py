@@ -248,14 +248,17 @@ class PrelimSearch:
             q.close()
 
     def set_tuning(self, stage_bytes: int = 0, tile_residues: int = 0, max_warps_per_block: int = 0,
-                   launch_mode: int = 0):
+                   launch_mode: int = 0, batch_launch: int = 0):
         """Launch shape (0 = library default for each); launch_mode 0: CUDA
-        graph for batched runs, 1: direct launches, 2: CUDA graph always."""
+        graph for batched runs, 1: direct launches, 2: CUDA graph always;
+        batch_launch 0: by database size, 1: tiles of many queries per
+        launch, 2: one scan launch per query."""
         self._auto = False
-        self._set_tuning(stage_bytes, tile_residues, max_warps_per_block, launch_mode)
+        self._set_tuning(stage_bytes, tile_residues, max_warps_per_block, launch_mode, batch_launch)
 
-    def _set_tuning(self, stage_bytes=0, tile_residues=0, max_warps_per_block=0, launch_mode=0):
-        t = BlazeTuning(int(stage_bytes), int(tile_residues), int(max_warps_per_block), int(launch_mode))
+    def _set_tuning(self, stage_bytes=0, tile_residues=0, max_warps_per_block=0, launch_mode=0, batch_launch=0):
+        t = BlazeTuning(int(stage_bytes), int(tile_residues), int(max_warps_per_block), int(launch_mode),
+                        int(batch_launch))
         check(self._lib.blaze_search_set_tuning(self._h, ctypes.byref(t)), "blaze_search_set_tuning")
 
     @property

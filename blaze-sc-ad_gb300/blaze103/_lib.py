@@ -65,7 +65,8 @@ class BlazeParams(ctypes.Structure):
 
 class BlazeTuning(ctypes.Structure):
     _fields_ = [("stage_bytes", ctypes.c_uint32), ("tile_residues", ctypes.c_uint32),
-                ("max_warps_per_block", ctypes.c_uint32), ("launch_mode", ctypes.c_uint32)]
+                ("max_warps_per_block", ctypes.c_uint32), ("launch_mode", ctypes.c_uint32),
+                ("batch_launch", ctypes.c_uint32)]
 
 
 class BlazeStats(ctypes.Structure):

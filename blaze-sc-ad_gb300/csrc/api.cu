@@ -320,6 +320,7 @@ struct RunSpec {
     const blaze_batch *b = nullptr;
     const blaze_params *p = nullptr;
     std::vector<int32_t> smin;  // per query: the reap's lowest kept score
+    std::vector<uint32_t> border;  // batched: query indices in launch (length) order
 };
 
 // One pass of both stages; fills s->h_cnt.
@@ -329,6 +330,7 @@ struct ScanLaunch {
     ScanArgs sa;
     int blocks, warps_per_block;
     size_t smem_bytes;
+    bool tiles;  // the batched (tiled) kernel, else the single-query one
 };
 
 struct PassLaunch {
@@ -344,7 +346,7 @@ static cudaError_t enqueue_pass(blaze_search *s, const PassLaunch &pl, unsigned 
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(s->ev[1], s->stream, event_flags);
     for (const ScanLaunch &l : pl.scans) {
         if (e != cudaSuccess) break;
-        e = pl.batched ? launch_scan_batch(l.sa, l.blocks, l.warps_per_block, l.smem_bytes, s->stream)
+        e = l.tiles ? launch_scan_batch(l.sa, l.blocks, l.warps_per_block, l.smem_bytes, s->stream)
                        : launch_scan(l.sa, l.blocks, l.warps_per_block, l.smem_bytes, s->stream);
     }
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(s->ev[2], s->stream, event_flags);
@@ -428,6 +430,7 @@ struct ScanPlan {
     int blocks = 0;
     uint32_t first = 0, n = 1;
     uint32_t tile_residues = 0;
+    bool tiles = false;  // batched: tiles of the plan's queries; else one query's launch
 };
 
 // Subject ranges of about `target` residues, from the longest subjects down
@@ -518,7 +521,23 @@ static int run_pass(blaze_search *s, const RunSpec &r, const std::vector<ScanPla
         sa.work_cap = work_cap;
         sa.cnt = s->d_cnt;
         sa.cursor = s->cursors.p + pl.scans.size();
-        if (batched) {
+        l.tiles = plan.tiles;
+        if (batched && !plan.tiles) {
+            // one query of the batch with the single-query kernel; its work
+            // items carry the query's batch index
+            const uint32_t i = r.border[plan.first];
+            const blaze_batch *b = r.b;
+            sa.q = b->d_res + b->res_off[i];
+            sa.qlen = b->qlen[i];
+            sa.cell_start = b->d_cell_start + static_cast<size_t>(i) * (kWords + 1);
+            sa.cell_pack = b->d_cell_pack + static_cast<size_t>(i) * kWords;
+            sa.presence = b->d_presence + static_cast<size_t>(i) * kPresenceWords;
+            sa.cell_off = b->d_cell_off + b->off_off[i];
+            sa.cutoff = r.p[i].ungapped_cutoff;
+            sa.n_queries = 1;
+            sa.query_index = i;
+            sa.work_query = s->work_query.p;
+        } else if (batched) {
             sa.queries = s->bq.p + plan.first;
             sa.n_queries = plan.n;
             // a tile is one block's work: tile_residues per warp
@@ -671,19 +690,27 @@ static int run_search(blaze_search *s, const RunSpec &spec, uint64_t *n_hsps) {
         while (k < 4 && need > kSteps[k]) ++k;
         return k + (qlen > kQuerySmemMax ? 8 : 0);  // longer queries stay in global memory: own launch
     };
+    // batched runs on a large database launch the single-query kernel once
+    // per query (a query alone fills the GPU there, and that kernel is the
+    // faster per residue); the tiles pay off where per-query launches are short
+    constexpr uint64_t kPerQueryLaunchResidues = 1ull << 27;
+    const bool per_query = batched && (s->batch_launch == 2 ||
+                                       (s->batch_launch == 0 && db->total >= kPerQueryLaunchResidues));
+    r.border = order;
     for (uint32_t i = 0; i < nq;) {
         uint32_t j = i + 1;
-        if (batched) {
+        if (batched && !per_query) {
             const int step = smem_step(qlen_at(i));
             while (j < nq && smem_step(qlen_at(j)) == step) ++j;
         }
         ScanPlan pl;
-        pl.lay = batched ? batch_layout_for(qlen_at(j - 1)) : layout_for(qlen_at(j - 1));
+        pl.tiles = batched && !per_query;
+        pl.lay = pl.tiles ? batch_layout_for(qlen_at(j - 1)) : layout_for(qlen_at(j - 1));
         pl.first = i;
         pl.n = j - i;
         if (pl.lay.smem_bytes > 227 * 1024 - 64) return BLAZE_ERR_LIMIT;  // the opt-in limit less static shared memory
         int per_sm = 0;
-        if (batched) {
+        if (pl.tiles) {
             BLAZE_CUDA_TRY(scan_batch_occupancy(pl.lay.query_smem_bytes != 0, pl.lay.warps_per_block, pl.lay.smem_bytes,
                                                 &per_sm));
         } else {
@@ -691,7 +718,7 @@ static int run_search(blaze_search *s, const RunSpec &spec, uint64_t *n_hsps) {
         }
         if (per_sm < 1) return BLAZE_ERR_LIMIT;
         pl.blocks = s->n_sm * per_sm;
-        if (batched) {
+        if (pl.tiles) {
             if (s->tile_residues) {
                 pl.tile_residues = s->tile_residues;
             } else {
@@ -964,8 +991,9 @@ extern "C" int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t) t
     if (!s || !t) return BLAZE_ERR_INVALID_ARG;
     if (t->stage_bytes > 16384 || t->max_warps_per_block > static_cast<uint32_t>(kScanMaxWarpsPerBlock))
         return BLAZE_ERR_LIMIT;
-    if (t->launch_mode > 2) return BLAZE_ERR_INVALID_ARG;
+    if (t->launch_mode > 2 || t->batch_launch > 2) return BLAZE_ERR_INVALID_ARG;
     s->launch_mode = t->launch_mode;
+    s->batch_launch = t->batch_launch;
     s->stage_bytes = t->stage_bytes ? t->stage_bytes : kScanStageBytes;
     s->tile_residues = t->tile_residues;
     s->max_warps = t->max_warps_per_block;

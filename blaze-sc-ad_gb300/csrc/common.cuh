@@ -118,6 +118,7 @@ struct ScanArgs {
     const uint32_t *tile_bounds;  // n_ranges + 1 subject indices, descending: range r is [b[r+1], b[r])
     uint32_t n_ranges;
     uint32_t *work_query;        // query index of each work item (nullptr: one query)
+    uint32_t query_index;        // single-query launches inside a batched pass: the query's index
     InitHit *scratch;          // per warp: scratch_cap records
     uint32_t scratch_cap;
     InitHit *init_out;

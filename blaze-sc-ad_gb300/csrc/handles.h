@@ -91,6 +91,7 @@ struct blaze_search {
     std::map<uint32_t, uint32_t> tile_ranges;
     uint32_t max_warps = 0;
     uint32_t launch_mode = 0;
+    uint32_t batch_launch = 0;  // blaze_tuning.batch_launch
     // the per-pass launch sequence as a CUDA graph, and the arguments it was
     // captured with
     cudaGraphExec_t graph_exec = nullptr;

@@ -711,7 +711,8 @@ scan_kernel(const ScanArgs a) {
         const uint32_t subj = a.n_subj - 1 - static_cast<uint32_t>(t);
         const bool staged = stage_issue(f, a, stage, 0, subj);
         if (staged && !stage_wait(f, a, 0)) return;
-        process_subject<QS, true>(f, a, c, q, subj, 0u, staged ? stage : kNoStage, word_hits, residues);
+        process_subject<QS, true>(f, a, c, q, subj, a.query_index, staged ? stage : kNoStage, word_hits,
+                                  residues);
     }
     finish_counters(a, f, word_hits, residues);
 }

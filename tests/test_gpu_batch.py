@@ -76,7 +76,9 @@ def test_batch_equals_plain_per_query():
             assert np.array_equal(g[f], ref[f]), f
 
 
-@pytest.mark.parametrize("tuning", [dict(tile_residues=1), dict(tile_residues=1 << 24),
+@pytest.mark.parametrize("tuning", [dict(batch_launch=2), dict(batch_launch=1, tile_residues=64),
+                                    dict(batch_launch=2, launch_mode=1, stage_bytes=256),
+                                    dict(tile_residues=1), dict(tile_residues=1 << 24),
                                     dict(stage_bytes=512, max_warps_per_block=3),
                                     dict(stage_bytes=8192, tile_residues=3000)])
 def test_batch_tuning_does_not_change_results(tuning):
