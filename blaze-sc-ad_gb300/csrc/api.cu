@@ -690,12 +690,15 @@ static int run_search(blaze_search *s, const RunSpec &spec, uint64_t *n_hsps) {
         while (k < 4 && need > kSteps[k]) ++k;
         return k + (qlen > kQuerySmemMax ? 8 : 0);  // longer queries stay in global memory: own launch
     };
-    // batched runs on a large database launch the single-query kernel once
-    // per query (a query alone fills the GPU there, and that kernel is the
-    // faster per residue); the tiles pay off where per-query launches are short
+    // batched runs of few queries, or on a large database, launch the
+    // single-query kernel once per query (a query alone fills the GPU there,
+    // and that kernel is the faster per residue); the tiles pay off where
+    // many per-query launches would each be short
     constexpr uint64_t kPerQueryLaunchResidues = 1ull << 27;
+    constexpr uint32_t kPerQueryLaunchQueries = 16;
     const bool per_query = batched && (s->batch_launch == 2 ||
-                                       (s->batch_launch == 0 && db->total >= kPerQueryLaunchResidues));
+                                       (s->batch_launch == 0 && (db->total >= kPerQueryLaunchResidues ||
+                                                                 nq <= kPerQueryLaunchQueries)));
     r.border = order;
     for (uint32_t i = 0; i < nq;) {
         uint32_t j = i + 1;

@@ -271,10 +271,11 @@ typedef struct blaze_tuning {
      * The graph is captured once and replayed while the launch arguments stay
      * the same (updated in place when they change). */
     uint32_t launch_mode;
-    /* Batched runs: 0: by database size (one scan launch per query from
-     * 2^27 residues on, where a query alone fills the GPU; tiles of many
-     * queries per launch below); 1: tiles always; 2: one launch per query
-     * always. Results are identical either way. */
+    /* Batched runs: 0: automatic (one scan launch per query for batches of
+     * at most 16 queries or databases from 2^27 residues on, where a query
+     * alone fills the GPU; tiles of many queries per launch otherwise);
+     * 1: tiles always; 2: one launch per query always. Results are
+     * identical either way. */
     uint32_t batch_launch;
 } blaze_tuning;
 int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t);
