@@ -422,9 +422,10 @@ static int launch_pass_graph(blaze_search *s, const PassLaunch &pl) {
     return BLAZE_OK;
 }
 
-// One scan launch of a pass: the single-query kernel, or the batched kernel
-// over one length class of a batch (queries [first, first + n) of the
-// class-ordered descriptors), each with its own shared-memory layout.
+// One scan launch of a pass: the single-query kernel (a single-query run, or
+// one query of a batch), or the batched kernel over a group of a batch's
+// queries (queries [first, first + n) of the length-ordered descriptors),
+// each with its own shared-memory layout.
 struct ScanPlan {
     ScanLayout lay;
     int blocks = 0;
