@@ -195,3 +195,114 @@ def test_length_adjustment_fixed_point(oracle_mod):
         assert f(ell) > ell
         nxt = ell + 1
         assert not (f(nxt) > nxt and K * (m - nxt) * (n - N * nxt) > max(m, n))
+
+
+# ------------------------------------------- word finder, two-hit, ungapped
+
+def _py_init_hits(q, sub, threshold, window, xdrop, cutoff):
+    """Independent restatement of the preliminary stage's word finder for one
+    subject, from the published two-hit method: neighbourhood words by brute
+    force; per diagonal the last hit and a flag set after a right extension
+    (hits before its end are skipped, the first one past it starts over); a
+    hit 3 to window-1 positions after the last one triggers the ungapped X-drop
+    extension (left from the end of the word's best prefix; right only when the
+    left walk reached the first hit, stopping at score <= 0)."""
+    m = BLOSUM62.astype(np.int64)
+    alpha = np.arange(28)
+    X, Y, Z = np.meshgrid(alpha, alpha, alpha, indexing="ij")
+    X, Y, Z = X.ravel(), Y.ravel(), Z.ravel()
+    look = {}
+    for i in range(len(q) - 2):
+        a, b, c = int(q[i]), int(q[i + 1]), int(q[i + 2])
+        sc = m[a][X] + m[b][Y] + m[c][Z]
+        for v in np.flatnonzero((sc >= threshold) | ((X == a) & (Y == b) & (Z == c))):
+            look.setdefault(int(v), []).append(i)
+
+    def score(qi, si):
+        return int(m[q[qi], sub[si]])
+
+    def extend(s_left, s_off, q_off):
+        sc = best = rd = 0
+        for i in range(3):
+            sc += score(q_off + i, s_off + i)
+            if sc > best:
+                best, rd = sc, i + 1
+        qr, sr = q_off + rd, s_off + rd
+        left = run = 0
+        best_k = -1
+        for k in range(min(sr - 1, qr - 1) + 1):  # left walk from (qr - 1, sr - 1)
+            run += score(qr - 1 - k, sr - 1 - k)
+            if run > left:
+                left, best_k = run, k
+            if left - run >= xdrop:
+                break
+        ld = best_k + 1
+        right, rlen, rext, slast = 0, 0, False, sr
+        if ld >= sr - s_left:
+            rext = True
+            n = min(len(sub) - sr, len(q) - qr)
+            run = right = left
+            best_i, i = -1, 0
+            while i < n:
+                run += score(qr + i, sr + i)
+                if run > right:
+                    right, best_i = run, i
+                if run <= 0 or right - run >= xdrop:
+                    break
+                i += 1
+            rlen, slast = best_i + 1, sr + i
+        return max(left, right), qr - ld, sr - ld, ld + rlen, rext, slast
+
+    hits, state = [], {}
+    for s in range(len(sub) - 2):
+        w = int(sub[s]) * 784 + int(sub[s + 1]) * 28 + int(sub[s + 2])
+        for qo in look.get(w, []):
+            d = s - qo
+            last, flag = state.get(d, (None, False))
+            if flag:
+                if s >= last:
+                    state[d] = (s, False)
+                continue
+            if last is None or s - last >= window:
+                state[d] = (s, False)
+                continue
+            if s - last < 3:
+                continue
+            sc, hq, hs, hl, rext, slast = extend(last + 3, s, qo)
+            if sc >= cutoff:
+                hits.append((hq, hs, hl, sc, qo, s))
+            state[d] = (slast - 2, True) if rext else (s, False)
+    return hits
+
+
+@pytest.mark.parametrize("seed", range(30))
+def test_init_hits_match_independent_restatement(oracle_mod, seed):
+    rng = np.random.default_rng(900 + seed)
+    q = synth.random_residues(rng, int(rng.integers(50, 160)))
+    if seed % 3 == 0:  # a low-complexity stretch: dense same-diagonal hits
+        q[10:40] = np.array([1, 11, 17], dtype=np.uint8)[rng.integers(0, 3, 30)]
+    seqs = []
+    for i in range(12):
+        s = synth.random_residues(rng, int(rng.integers(20, 400)))
+        if i % 3 == 0 and len(q) > 30:
+            w = int(rng.integers(20, len(q)))
+            s0 = int(rng.integers(0, len(q) - w + 1))
+            hom = synth.mutate(rng, q[s0:s0 + w], float(rng.uniform(0.4, 0.9)))
+            p = int(rng.integers(0, len(s) + 1))
+            s = np.concatenate([s[:p], hom, s[p:]])
+        seqs.append(s)
+    off = np.zeros(len(seqs) + 1, dtype=np.uint64)
+    off[1:] = np.cumsum([len(s) for s in seqs])
+    res = np.concatenate(seqs)
+    p = oracle_mod.default_params(len(q), 50_000_000, 100_000)
+    _, ini = oracle_mod.search_db(q, res, off, p, threads=1, want_inits=True)
+    total = 0
+    for k, s in enumerate(seqs):
+        want = sorted(_py_init_hits(q, s, p["word_threshold"], p["window"], p["ungapped_xdrop"],
+                                    p["ungapped_cutoff"]))
+        mine = ini[ini["subject"] == k]
+        got = sorted(zip(*(mine[f].tolist() for f in ("q_start", "s_start", "len", "score", "q_trig", "s_trig"))))
+        assert got == want, (seed, k)
+        total += len(want)
+    if seed % 3 == 0:
+        assert total > 0
