@@ -306,3 +306,67 @@ def test_init_hits_match_independent_restatement(oracle_mod, seed):
         total += len(want)
     if seed % 3 == 0:
         assert total > 0
+
+
+# ------------------------------------------------ gapped stage per subject
+
+def _py_gapped_subject(oracle_mod, q, s, inits, p):
+    """Independent restatement of the per-subject gapped pipeline over the
+    subject's init hits: order by ungapped score (ties in discovery order),
+    skip an init hit inside a kept HSP at least as good, X-drop DP left and
+    right of the gapped start point (the DP itself is checked by brute force
+    above), keep what reaches the gapped cutoff, then drop HSPs sharing a
+    start and then an end with a better one, and order by score."""
+    order = sorted(inits, key=lambda u: (-u["score"], u["s_trig"], u["q_trig"]))
+    kept = []
+    for u in order:
+        if any(u["score"] <= g["score"] and g["q_start"] <= u["q_start"] and u["q_start"] + u["len"] <= g["q_end"]
+               and g["s_start"] <= u["s_start"] and u["s_start"] + u["len"] <= g["s_end"] for g in kept):
+            continue
+        qo = oracle_mod.gapped_start(q, s, u["q_start"], u["s_start"], u["len"])
+        so = qo + u["s_start"] - u["q_start"]
+        gx = dict(gap_open=p["gap_open"], gap_extend=p["gap_extend"], xdrop=p["gapped_xdrop"])
+        left, al, bl = oracle_mod.semi_gapped(q, s, qo + 1, so + 1, True, **gx)
+        right, ar, br = 0, 0, 0
+        if qo < len(q) - 1 and so < len(s) - 1:
+            right, ar, br = oracle_mod.semi_gapped(q[qo:], s[so:], len(q) - qo - 1, len(s) - so - 1, False, **gx)
+        if left + right >= p["gapped_cutoff"]:
+            kept.append(dict(score=left + right, q_start=qo + 1 - al, q_end=qo + ar + 1, s_start=so + 1 - bl,
+                             s_end=so + br + 1, q_gstart=qo, s_gstart=so))
+    by_start = sorted(kept, key=lambda h: (h["q_start"], h["s_start"], -h["score"], -h["q_end"], -h["s_end"]))
+    m = [h for i, h in enumerate(by_start)
+         if i == 0 or (h["q_start"], h["s_start"]) != (by_start[i - 1]["q_start"], by_start[i - 1]["s_start"])]
+    by_end = sorted(m, key=lambda h: (h["q_end"], h["s_end"], -h["score"], h["q_start"], h["s_start"]))
+    m = [h for i, h in enumerate(by_end)
+         if i == 0 or (h["q_end"], h["s_end"]) != (by_end[i - 1]["q_end"], by_end[i - 1]["s_end"])]
+    return sorted(m, key=lambda h: (-h["score"], h["s_start"], -h["s_end"], h["q_start"], -h["q_end"]))
+
+
+@pytest.mark.parametrize("seed", range(10))
+def test_gapped_hsps_match_independent_restatement(oracle_mod, seed):
+    rng = np.random.default_rng(1300 + seed)
+    q = synth.random_residues(rng, int(rng.integers(80, 300)))
+    seqs = []
+    for i in range(10):
+        s = synth.random_residues(rng, int(rng.integers(30, 500)))
+        for _ in range(int(rng.integers(0, 3))):  # several homologous stretches, some overlapping
+            w = int(rng.integers(20, len(q)))
+            s0 = int(rng.integers(0, len(q) - w + 1))
+            hom = synth.mutate(rng, q[s0:s0 + w], float(rng.uniform(0.4, 0.95)))
+            p0 = int(rng.integers(0, len(s) + 1))
+            s = np.concatenate([s[:p0], hom, s[p0:]])
+        seqs.append(s)
+    off = np.zeros(len(seqs) + 1, dtype=np.uint64)
+    off[1:] = np.cumsum([len(s) for s in seqs])
+    res = np.concatenate(seqs)
+    p = oracle_mod.default_params(len(q), 20_000_000, 50_000)
+    hsps, ini = oracle_mod.search_db(q, res, off, p, threads=1, want_inits=True)
+    total = 0
+    for k, s in enumerate(seqs):
+        want = _py_gapped_subject(oracle_mod, q, s, [dict(zip(ini.dtype.names, r.tolist()))
+                                                     for r in ini[ini["subject"] == k]], p)
+        got = hsps[hsps["subject"] == k]
+        fields = ["score", "q_start", "q_end", "s_start", "s_end", "q_gstart", "s_gstart"]
+        assert [tuple(int(g[f]) for f in fields) for g in got] == [tuple(h[f] for f in fields) for h in want], (seed, k)
+        total += len(want)
+    assert total > 0
