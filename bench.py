@@ -201,7 +201,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic (seeded; plain-db-scale workload: 8 queries, 2M subjects)",
+        "data": f"synthetic (seeded; plain-db-scale workload: 8 queries, {w.n_subjects} subjects)",
         "config": {"workload": "plain drop-in, 8 queries (100-1000 aa) vs 2M subjects / 0.7G residues",
                    "db_subjects": w.n_subjects, "db_residues": w.total_residues,
                    "queries": [len(q) for q in w.queries], "parallelism": "host threads",
