@@ -743,7 +743,7 @@ static int run_search(blaze_search *s, const RunSpec &spec, uint64_t *n_hsps) {
     }
 
     if (batched) {
-        // per-query descriptors of this run in class order (cutoffs come from
+        // per-query descriptors of this run in length order (cutoffs come from
         // the parameters); the per-query arrays of the gapped stage stay in
         // batch order
         std::vector<BatchQuery> bq(nq);
