@@ -20,3 +20,13 @@ def oracle_mod():
 
     oracle.build()
     return oracle
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built_library():
+    """Builds libblaze103 (nvcc, sm_103a) when a fresh checkout runs the tests
+    before the build step; the library itself never falls back to anything."""
+    if not os.path.exists(os.path.join(PKG, "blaze103", "libblaze103.so")):
+        import build as pkg_build  # blaze-sc-ad_gb300/build.py
+
+        pkg_build.build()
