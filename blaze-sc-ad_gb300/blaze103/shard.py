@@ -57,9 +57,42 @@ def merge(parts, bases) -> np.ndarray:
     return cat[np.lexsort(keys)]  # lexsort is stable: per-subject order is kept
 
 
-def gather_merge(local_hsps: np.ndarray, base: int, group=None, dst: int = 0):
+def keep_best_subjects(hsps: np.ndarray, hitlist_size: int) -> np.ndarray:
+    """hitlist_size (NCBI max_target_seqs) over merged records: per query,
+    the hitlist_size subjects whose lists start with the best score (E-values
+    of one query fall with the score), ties by smaller OID -- the rule each
+    rank's device selection applies to its own shard. Every subject of the
+    global top k is in its own rank's top k, so culling each shard and then
+    the merge gives exactly the lists of one search over the whole database.
+    Records must be grouped by (query,) OID with each list best first, as
+    merge() returns them."""
+    if hitlist_size <= 0 or len(hsps) == 0:
+        return hsps
+    batched = "query" in hsps.dtype.names
+    qcol = hsps["query"].astype(np.int64) if batched else np.zeros(len(hsps), dtype=np.int64)
+    oid = hsps["oid"].astype(np.int64)
+    # first record of each (query, OID) list carries its best score
+    start = np.ones(len(hsps), dtype=bool)
+    start[1:] = (qcol[1:] != qcol[:-1]) | (oid[1:] != oid[:-1])
+    heads = np.flatnonzero(start)
+    hq, ho, hs = qcol[heads], oid[heads], hsps["score"][heads].astype(np.int64)
+    order = np.lexsort((ho, -hs, hq))  # by query, then best score descending, then OID
+    rank_in_query = np.empty(len(order), dtype=np.int64)
+    sq = hq[order]
+    first_of_query = np.ones(len(order), dtype=bool)
+    first_of_query[1:] = sq[1:] != sq[:-1]
+    group_start = np.maximum.accumulate(np.where(first_of_query, np.arange(len(order)), 0))
+    rank_in_query[order] = np.arange(len(order)) - group_start
+    keep_head = rank_in_query < hitlist_size
+    list_id = np.cumsum(start) - 1
+    return hsps[keep_head[list_id]]
+
+
+def gather_merge(local_hsps: np.ndarray, base: int, group=None, dst: int = 0, hitlist_size: int = 0):
     """torch.distributed gather of every rank's records to rank `dst`, which
-    returns the merged array; other ranks return None."""
+    returns the merged array (with hitlist_size > 0: culled to the best
+    hitlist_size subjects per query over the whole database); other ranks
+    return None."""
     import torch.distributed as dist
 
     rank = dist.get_rank(group)
@@ -69,13 +102,17 @@ def gather_merge(local_hsps: np.ndarray, base: int, group=None, dst: int = 0):
     dist.gather_object(payload, got, dst=dst, group=group)
     if rank != dst:
         return None
-    return merge([g[1] for g in got], [g[0] for g in got])
+    return keep_best_subjects(merge([g[1] for g in got], [g[0] for g in got]), hitlist_size)
 
 
-def sharded_search(residues, offsets, queries, evalue: float = 10.0, group=None, device: int | None = None):
+def sharded_search(residues, offsets, queries, evalue: float = 10.0, group=None, device: int | None = None,
+                   hitlist_size: int = 0, max_hsps: int = 0):
     """Searches each query against this rank's shard of the database on its
     GPU and gathers the merged per-subject HSP lists to rank 0 (None
-    elsewhere). Every rank passes the same residues/offsets."""
+    elsewhere). Every rank passes the same residues/offsets. hitlist_size and
+    max_hsps cull as one search over the whole database would: max_hsps is
+    per subject, so each rank applies it; hitlist_size is applied on each
+    rank's device and again over the merge."""
     import torch.distributed as dist
 
     import blaze103
@@ -90,8 +127,9 @@ def sharded_search(residues, offsets, queries, evalue: float = 10.0, group=None,
     try:
         for q in queries:
             p = blaze103.default_params(len(q), evalue=evalue, db_residues=total, db_subjects=n)
+            p.hitlist_size, p.max_hsps = int(hitlist_size), int(max_hsps)
             local = ps.run(q, p).hsps if hi > lo else np.empty(0, dtype=blaze103.HSP_DTYPE)
-            results.append(gather_merge(local, lo, group))
+            results.append(gather_merge(local, lo, group, hitlist_size=hitlist_size))
     finally:
         ps.close()
         src.close()

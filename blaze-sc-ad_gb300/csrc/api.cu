@@ -796,7 +796,9 @@ static int run_search(blaze_search *s, const RunSpec &spec, uint64_t *n_hsps) {
             BLAZE_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev[2], s->ev[3]));
             s->stats.gapped_ms = ms;
         }
-        if (c.flags & kFlagBadState) return BLAZE_ERR_INTERNAL;
+        // the DP rows fit the longest subject and the scan's init hits lie in
+        // their sequences, so these two are consistency failures here
+        if (c.flags & (kFlagBadState | kFlagSubjectTooLong | kFlagBadInitHit)) return BLAZE_ERR_INTERNAL;
         bool again = false;
         if (c.overflow_subjects > 0) {
             s->scratch_cap = std::max<uint32_t>(s->scratch_cap * 2, c.max_init_needed + 64);

@@ -84,6 +84,8 @@ constexpr unsigned kFlagWorkArrayFull = 2u;
 constexpr unsigned kFlagOutArrayFull = 4u;
 constexpr unsigned kFlagSavedFull = 8u;
 constexpr unsigned kFlagBadState = 16u;
+constexpr unsigned kFlagSubjectTooLong = 32u;  // gapped: a subject longer than its DP rows was skipped
+constexpr unsigned kFlagBadInitHit = 64u;      // gapped: an init hit outside its query or subject was skipped
 
 // One query of a batch, as the batched scan kernel reads it.
 struct BatchQuery {
@@ -221,7 +223,8 @@ ScanLayout scan_layout(int32_t qlen, int32_t window, uint32_t stage_bytes, size_
 cudaError_t launch_scan(const ScanArgs &a, int n_blocks, int warps_per_block, size_t smem, cudaStream_t st);
 cudaError_t scan_occupancy(bool query_in_smem, int warps_per_block, size_t smem, int *blocks_per_sm);
 int scan_max_warps_by_registers(bool query_in_smem);
-cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st);
+cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st,
+                          int warps_per_block = kGappedWarpsPerBlock);
 cudaError_t launch_hitlist(const HitlistArgs &a, uint32_t n_select, int n_sm, cudaStream_t st);
 constexpr int kTracebackWarpsPerBlock = 4;
 cudaError_t launch_traceback(const TracebackArgs &a, int n_blocks, cudaStream_t st);

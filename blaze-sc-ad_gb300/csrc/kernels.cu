@@ -288,22 +288,42 @@ gapped_kernel(const GappedArgs a) {
         const InitHit *in = a.init_in + wi.first;
         const uint64_t o0 = a.off[wi.subject];
         const uint8_t *sub = a.res + o0;
-        const int32_t slen = static_cast<int32_t>(a.off[wi.subject + 1] - o0);
+        const uint64_t o1 = a.off[wi.subject + 1];
         if (n > a.cap) {  // cannot happen: the scan kernel only publishes n <= its scratch cap
             if (lane == 0) atomicOr(&a.cnt->flags, kFlagBadState);
             continue;
         }
-        // order: score descending, ties in discovery order (rank sort)
+        // The DP rows hold dp_stride ints: a subject too long for them (only
+        // possible where the caller sized the rows, as the allocation-free
+        // entry point does) is skipped and reported.
+        if (o1 < o0 || o1 - o0 + 2u > a.dp_stride) {
+            if (lane == 0) atomicOr(&a.cnt->flags, kFlagSubjectTooLong);
+            continue;
+        }
+        const int32_t slen = static_cast<int32_t>(o1 - o0);
+        // order: score descending, ties in discovery order (rank sort; equal
+        // records, which only a caller can pass, keep their input order, so
+        // every slot is written)
         for (uint32_t i = lane; i < n; i += 32) {
             const InitHit hi = in[i];
             uint32_t rank = 0;
-            for (uint32_t j = 0; j < n; ++j) rank += init_before(in[j], hi) ? 1u : 0u;
+            for (uint32_t j = 0; j < n; ++j) {
+                const InitHit hj = in[j];
+                rank += (init_before(hj, hi) || (j < i && !init_before(hi, hj))) ? 1u : 0u;
+            }
             sorted[rank] = hi;
         }
         __syncwarp();
         int nsaved = 0;
         for (uint32_t k = 0; k < n; ++k) {
             const InitHit u = sorted[k];
+            // an init hit must lie inside the query and the subject (the scan
+            // kernel's always do; a caller's may not): others are skipped
+            if (u.len < 1 || u.q_start < 0 || u.s_start < 0 || u.len > qlen - u.q_start ||
+                u.len > slen - u.s_start) {
+                if (lane == 0) atomicOr(&a.cnt->flags, kFlagBadInitHit);
+                continue;
+            }
             bool inside = false;
             for (int j = lane; j < nsaved; j += 32) {
                 const DevHsp g = saved[j];
@@ -455,8 +475,9 @@ cudaError_t launch_hitlist(const HitlistArgs &a, uint32_t n_select, int n_sm, cu
     return cudaGetLastError();
 }
 
-cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st) {
-    gapped_kernel<<<n_blocks, kGappedWarpsPerBlock * 32, 0, st>>>(a);
+cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st, int warps_per_block) {
+    if (warps_per_block < 1 || warps_per_block > kGappedWarpsPerBlock) return cudaErrorInvalidValue;
+    gapped_kernel<<<n_blocks, warps_per_block * 32, 0, st>>>(a);
     return cudaGetLastError();
 }
 

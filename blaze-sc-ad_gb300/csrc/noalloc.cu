@@ -16,9 +16,11 @@ using namespace blaze;
 
 namespace {
 
-// Fixed shape of the gapped kernel in this mode: 76 blocks of 4 warps.
-constexpr int kBlocks = 76;
-constexpr int kWarps = kBlocks * kGappedWarpsPerBlock;                  // 304
+// Fixed shape of the gapped kernel in this mode: 304 warps, as 152 blocks of
+// two warps so that every SM of a GB300 takes a share of the work.
+constexpr int kWarpsPerBlock = 2;
+constexpr int kBlocks = 152;
+constexpr int kWarps = kBlocks * kWarpsPerBlock;                         // 304
 constexpr uint32_t kMaxInit = BLAZE_NOALLOC_MAX_INIT_HITS;             // per subject
 constexpr uint32_t kDpStride = BLAZE_NOALLOC_MAX_SUBJECT_LENGTH + 2;   // ints per DP row
 constexpr size_t kCountersBytes = 256;
@@ -32,26 +34,75 @@ static_assert(sizeof(blaze_dev_init_hit) == sizeof(InitHit), "init hit layout");
 static_assert(sizeof(blaze_dev_subject) == sizeof(WorkItem), "subject group layout");
 static_assert(sizeof(blaze_dev_hsp) == sizeof(DevHsp), "HSP layout");
 static_assert(offsetof(blaze_dev_subject, first_init_hit) == offsetof(WorkItem, first), "group layout");
+static_assert(BLAZE_NOALLOC_OUTPUT_CUT == kFlagOutArrayFull && BLAZE_NOALLOC_TOO_MANY_INIT_HITS == kFlagBadState &&
+                  BLAZE_NOALLOC_SUBJECT_TOO_LONG == kFlagSubjectTooLong &&
+                  BLAZE_NOALLOC_BAD_INIT_HIT == kFlagBadInitHit,
+              "status bits of d_result[1]");
 
 // The working memory of every call, on every device that loads the library.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[BLAZE_NOALLOC_SCRATCH_BYTES];
 
-// Device address of g_noalloc_scratch per device, looked up once per device.
+// Device address of g_noalloc_scratch, looked up once per CUDA context: the
+// cache is keyed by the context's process-unique ID, so a context that was
+// destroyed (cudaDeviceReset) and created again gets a fresh lookup. The
+// driver's context calls are reached through the runtime's entry-point
+// query, so the library links no driver library.
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 unsigned char *g_scratch_addr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};
 
-int scratch_address(int device, unsigned char **out) {
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[device]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+using CtxGetCurrentFn = int (*)(void **ctx);
+using CtxGetIdFn = int (*)(void *ctx, unsigned long long *id);
+
+int current_context_id(unsigned long long *id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaDriverEntryPointQueryResult r1{}, r2{};
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &r1);
+        if (e == cudaSuccess)
+            e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &r2);
         if (e != cudaSuccess) {
             last_cuda_error(e);
             return BLAZE_ERR_CUDA;
         }
-        g_scratch_addr[device] = static_cast<unsigned char *>(p);
+        if (r1 != cudaDriverEntryPointSuccess || r2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return BLAZE_ERR_CUDA;
+        get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        get_id = reinterpret_cast<CtxGetIdFn>(f2);
     }
+    void *ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx || get_id(ctx, id) != 0) return BLAZE_ERR_CUDA;
+    return BLAZE_OK;
+}
+
+// Called with `device` current. A cached address is reused only while the
+// current context is the one it was looked up in; the first lookup of a
+// context goes through cudaGetSymbolAddress, which also initialises the
+// context when nothing has yet.
+int scratch_address(int device, unsigned char **out) {
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    unsigned long long ctx = 0;
+    if (g_scratch_addr[device]) {
+        int rc = current_context_id(&ctx);
+        if (rc != BLAZE_OK) return rc;
+        if (ctx == g_scratch_ctx[device]) {
+            *out = g_scratch_addr[device];
+            return BLAZE_OK;
+        }
+    }
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // creates the context if needed
+    if (e != cudaSuccess) {
+        last_cuda_error(e);
+        return BLAZE_ERR_CUDA;
+    }
+    int rc = current_context_id(&ctx);
+    if (rc != BLAZE_OK) return rc;
+    g_scratch_addr[device] = static_cast<unsigned char *>(p);
+    g_scratch_ctx[device] = ctx;
     *out = g_scratch_addr[device];
     return BLAZE_OK;
 }
@@ -113,7 +164,7 @@ extern "C" int blaze_gapped_noalloc(const uint8_t *d_residues, const uint64_t *d
     ga.out = reinterpret_cast<DevHsp *>(d_out);
     ga.out_cap = out_capacity;
     ga.cnt = cnt;
-    BLAZE_CUDA_TRY(launch_gapped(ga, kBlocks, st));
+    BLAZE_CUDA_TRY(launch_gapped(ga, kBlocks, st, kWarpsPerBlock));
     BLAZE_CUDA_TRY(cudaMemcpyAsync(d_result, &cnt->out_count, sizeof(uint64_t),
                                    cudaMemcpyDeviceToDevice, st));
     BLAZE_CUDA_TRY(cudaMemcpyAsync(d_result + 1, &cnt->flags, sizeof(cnt->flags),

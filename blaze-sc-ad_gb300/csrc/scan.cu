@@ -67,11 +67,11 @@ __device__ __forceinline__ int32_t score_of(uint32_t qa, uint32_t sb) {
 }
 
 // ------------------------------------------------------------------------
-// Subject staging by the bulk-copy (TMA) engine: one elected lane arms a
-// per-buffer mbarrier with the byte count and issues cp.async.bulk
-// global -> shared; the warp waits on the barrier's phase. Each warp has two
-// stage buffers, so the next subject's copy runs while the current one is
-// scanned. Waits are bounded: a copy that never lands sets kFlagBadState.
+// Subject staging by the bulk-copy (TMA) engine: one elected lane arms the
+// warp's mbarrier with the byte count and issues cp.async.bulk
+// global -> shared; the warp waits on the barrier's phase. A warp stages one
+// subject at a time, just before scanning it, in one stage buffer. Waits are
+// bounded: a copy that never lands sets kFlagBadState.
 
 constexpr uint32_t kBulkSpinLimit = 1u << 22;
 

@@ -344,20 +344,34 @@ int blaze_prelim_search(blaze_search *s, const uint8_t *query, int32_t length,
  * first record}. Output: finished HSPs (score order within a subject,
  * subjects in any order) in d_out; d_result[0] = HSPs produced (more than
  * out_capacity means the output was cut), d_result[1] = status bits
- * (0 = complete). Every subject must be at most max_subject_length residues
- * long and carry at most max_init_hits_per_subject init hits; values above
+ * (0 = complete; BLAZE_NOALLOC_* below). Every subject must be at most
+ * max_subject_length residues long and carry at most
+ * max_init_hits_per_subject init hits; values above
  * BLAZE_NOALLOC_MAX_SUBJECT_LENGTH / BLAZE_NOALLOC_MAX_INIT_HITS are rejected
- * with BLAZE_ERR_LIMIT.
+ * with BLAZE_ERR_LIMIT. The device checks each subject and init hit again:
+ * a subject longer than BLAZE_NOALLOC_MAX_SUBJECT_LENGTH or with more than
+ * BLAZE_NOALLOC_MAX_INIT_HITS init hits is skipped, and so is an init hit
+ * that does not lie inside the query and its subject (length >= 1); each
+ * such skip sets its status bit and the other subjects' HSPs are unchanged.
+ * Subject indices are not checked (the library does not know how many
+ * offsets d_offsets holds): each must be below that count.
  *
  * The call only enqueues work on `stream` (a cudaStream_t); read d_result
  * after synchronizing it. The first call on a device looks up the device
  * address of the fixed array, so make that first call before any stream
- * capture. All calls share the one array: calls whose work overlaps on the
+ * capture; the address is kept per CUDA context, so after a device reset
+ * (cudaDeviceReset) the next call looks it up again and should likewise come
+ * before any capture. All calls share the one array: calls whose work overlaps on the
  * GPU (other streams, other threads) race and must be serialized by the
  * caller. */
 #define BLAZE_NOALLOC_MAX_SUBJECT_LENGTH 4096u
 #define BLAZE_NOALLOC_MAX_INIT_HITS 128u
 #define BLAZE_NOALLOC_SCRATCH_BYTES (12u << 20)
+/* status bits of d_result[1] */
+#define BLAZE_NOALLOC_OUTPUT_CUT 4u          /* more HSPs than out_capacity */
+#define BLAZE_NOALLOC_TOO_MANY_INIT_HITS 16u /* a subject with too many init hits was skipped */
+#define BLAZE_NOALLOC_SUBJECT_TOO_LONG 32u   /* a subject over the length maximum was skipped */
+#define BLAZE_NOALLOC_BAD_INIT_HIT 64u       /* an init hit outside its sequences was skipped */
 
 typedef struct blaze_dev_init_hit {
     int32_t q_start, s_start, length, score;

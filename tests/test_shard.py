@@ -30,7 +30,7 @@ def _as_blaze(hsps):
     return out
 
 
-def _rank_main(rank, world, port, residues, offsets, query, outq):
+def _rank_main(rank, world, port, residues, offsets, query, outq, hitlist_size=0):
     import torch.distributed as dist
 
     import oracle
@@ -45,7 +45,10 @@ def _rank_main(rank, world, port, residues, offsets, query, outq):
         off = shard.shard_offsets(offsets, lo, hi)
         local_res = residues[int(off[0]):int(off[-1])]
         hs, _ = oracle.search_db(query, local_res, off - off[0], pd, threads=2)
-        merged = shard.gather_merge(_as_blaze(oracle.finish(hs, pd)), lo)
+        # with hitlist_size, each rank culls its own shard first, as its
+        # device selection would
+        local = oracle.cull(oracle.finish(hs, pd), hitlist_size=hitlist_size)
+        merged = shard.gather_merge(_as_blaze(local), lo, hitlist_size=hitlist_size)
         if rank == 0:
             outq.put(merged)
     finally:
@@ -64,23 +67,26 @@ def _workload(seed=3, n=600):
     return q, np.concatenate(seqs).astype(np.uint8), off
 
 
-@pytest.mark.parametrize("world", [2, 3])
-def test_sharded_merge_equals_whole_database(oracle_mod, world):
+@pytest.mark.parametrize("world,hitlist_size", [(2, 0), (3, 0), (2, 20)])
+def test_sharded_merge_equals_whole_database(oracle_mod, world, hitlist_size):
     q, res, off = _workload()
     pd = oracle_mod.default_params(len(q), int(off[-1]), len(off) - 1)
     hs, _ = oracle_mod.search_db(q, res, off, pd, threads=4)
-    want = _as_blaze(oracle_mod.finish(hs, pd))
+    want = _as_blaze(oracle_mod.cull(oracle_mod.finish(hs, pd), hitlist_size=hitlist_size))
+    if hitlist_size:
+        assert len(np.unique(want["oid"])) == hitlist_size
     ctx = mp.get_context("spawn")
     outq = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank_main, args=(r, world, port, res, off, q, outq)) for r in range(world)]
+    procs = [ctx.Process(target=_rank_main, args=(r, world, port, res, off, q, outq, hitlist_size))
+             for r in range(world)]
     for p in procs:
         p.start()
     got = outq.get(timeout=240)
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    assert len(want) > 50
+    assert len(want) > (19 if hitlist_size else 50)
     for f in blaze103.HSP_DTYPE.names:
         assert np.array_equal(got[f], want[f]), f
 
@@ -119,3 +125,17 @@ def test_merge_orders_batch_records():
     assert m["query"].tolist() == [0, 0, 0, 1, 1]
     assert m["oid"].tolist() == [0, 1, 10, 0, 10]
     assert m["score"].tolist() == [5, 6, 8, 7, 9]
+
+
+def test_keep_best_subjects_per_query():
+    a = np.zeros(7, dtype=blaze103.BATCH_HSP_DTYPE)
+    a["query"] = [0, 0, 0, 0, 1, 1, 1]
+    a["oid"] = [1, 1, 4, 9, 2, 3, 8]
+    a["score"] = [50, 20, 60, 50, 5, 7, 7]
+    k = shard.keep_best_subjects(a, 2)
+    assert k["query"].tolist() == [0, 0, 0, 1, 1]
+    assert k["oid"].tolist() == [1, 1, 4, 3, 8]  # query 0: 60 (oid 4), then 50 by smaller OID
+    assert len(shard.keep_best_subjects(a, 0)) == 7
+    single = np.zeros(3, dtype=blaze103.HSP_DTYPE)
+    single["oid"], single["score"] = [0, 5, 6], [9, 9, 10]
+    assert shard.keep_best_subjects(single, 2)["oid"].tolist() == [0, 6]
