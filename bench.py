@@ -16,9 +16,17 @@ e2e     the same metric through blaze_prelim_search with host query buffers:
 roofline  the scan kernel (word finder + two-hit + ungapped), HBM-bound:
         algorithmic bytes per launch = residues (1 B) + offsets (8 B each).
 
+parity  the oracle's HSPs for the cpu_baseline sample (every 4th subject,
+        whole-database statistics) compared field by field with the e2e
+        path's HSPs for the same OIDs.
+batched / serve  sub-records at N=1: the batched form on the 512-query,
+        5M-subject workload against the plain path on the same GPU (with
+        batched == plain and oracle checks on a subject sample), and the
+        serving loop's p50/p99 latency under Poisson arrivals.
+
 `--impl reference` times the CPU implementation of the path (the oracle port:
-NCBI blastp 2.13.0 is not installed on this machine) on the host cores, on a
-bounded sample of the same workload per step.
+NCBI blastp 2.13.0 is not installed on this machine) on the host cores, on the
+same bounded subject sample of the same workload per step as cpu_baseline.
 
 With N>1 (torchrun) every rank searches its own database of the same size
 (weak scaling, E-values over the global size) and the slowest rank's time
@@ -152,25 +160,84 @@ def measured_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def cpu_sample_run(workload, queries, frac: float, threads: int, db_total: int, db_n: int):
-    """Time the oracle on every k-th subject of the database (a bounded sample
-    with the same length distribution); returns (residues/s, seconds, residues)."""
-    import oracle
-
-    k = max(int(round(1.0 / frac)), 1)
+def subject_sample(workload, k: int):
+    """Every k-th subject of the database (a bounded sample with the same
+    length distribution): (OIDs, residues, offsets)."""
     off = workload.offsets
     idx = np.arange(0, workload.n_subjects, k)
     lens = (off[idx + 1] - off[idx]).astype(np.int64)
     sub_off = np.zeros(len(idx) + 1, dtype=np.uint64)
     np.cumsum(lens, out=sub_off[1:])
-    res = np.concatenate([workload.residues[int(off[i]):int(off[i + 1])] for i in idx])
+    if k == 1:
+        return idx, workload.residues, sub_off
+    res = workload.residues
+    return idx, np.concatenate([res[int(off[i]):int(off[i + 1])] for i in idx]), sub_off
+
+
+def cpu_sample_run(workload, queries, frac: float, threads: int, db_total: int, db_n: int, keep: bool = False):
+    """Time the oracle on every k-th subject of the database (k = 1/frac);
+    returns (residues/s, seconds, residues, subjects, sample). With keep, the
+    sample is (OIDs, per-query oracle HSPs with E-values and reap, subject =
+    position in the sample); the finishing step is outside the timed span."""
+    import oracle
+
+    k = max(int(round(1.0 / frac)), 1)
+    idx, res, sub_off = subject_sample(workload, k)
+    raw = []
     t0 = time.perf_counter()
     for q in queries:
         p = oracle.default_params(len(q), db_total, db_n)
-        oracle.search_db(q, res, sub_off, p, threads=threads)
+        hs, _ = oracle.search_db(q, res, sub_off, p, threads=threads)
+        raw.append((hs, p))
     dt = time.perf_counter() - t0
     n_res = int(sub_off[-1]) * len(queries)
-    return n_res / dt, dt, n_res, len(idx)
+    sample = (idx, [oracle.finish(hs, p) for hs, p in raw]) if keep else None
+    return n_res / dt, dt, n_res, len(idx), sample
+
+
+PARITY_FIELDS = [("oid", "subject"), ("score", "score"), ("q_start", "q_start"), ("q_end", "q_end"),
+                 ("s_start", "s_start"), ("s_end", "s_end"), ("q_gapped_start", "q_gstart"),
+                 ("s_gapped_start", "s_gstart")]
+
+
+def parity_check(idx, ref_lists, got_lists, k: int) -> dict:
+    """Field-by-field comparison of GPU HSPs (HSP_DTYPE, all subjects) with
+    the oracle's HSPs of the subject sample (OIDs idx = every k-th), per
+    query; a record counts as a mismatch when it is missing on either side
+    or differs in any field (E-values: relative 1e-12)."""
+    from collections import Counter
+
+    mism = hsps = ev_bad = 0
+    for ref, got in zip(ref_lists, got_lists):
+        g = got[(got["oid"] % k) == 0] if k > 1 else got
+        r = ref.copy()
+        r["subject"] = idx[r["subject"]].astype(r["subject"].dtype)
+        hsps += len(r)
+        if len(g) == len(r):
+            same = np.ones(len(r), dtype=bool)
+            for gf, rf in PARITY_FIELDS:
+                same &= g[gf].astype(np.int64) == r[rf].astype(np.int64)
+            if len(r):
+                ev_ok = np.abs(g["evalue"] - r["evalue"]) <= 1e-12 * np.abs(r["evalue"])
+                ev_bad += int((~ev_ok & same).sum())
+                same &= ev_ok
+            mism += int((~same).sum())
+            continue
+        tg = Counter(tuple(int(x[f]) for f, _ in PARITY_FIELDS) for x in g)
+        tr = Counter(tuple(int(x[f]) for _, f in PARITY_FIELDS) for x in r)
+        mism += sum(((tg - tr) + (tr - tg)).values())
+    return {"hsps": hsps, "mismatches": mism, "evalue_mismatches": ev_bad,
+            "fields": [f for f, _ in PARITY_FIELDS] + ["evalue (rtol 1e-12)"]}
+
+
+def plain_config(w, world) -> dict:
+    """The workload description both arms report (same config)."""
+    return {"workload": "plain drop-in: 8 queries (100-1000 aa) vs 2M subjects / 0.7G residues, "
+                        "one query per search",
+            "db_subjects": w.n_subjects, "db_residues": w.total_residues,
+            "queries": [len(q) for q in w.queries],
+            "parallelism": f"weak x{world} (one database per rank)" if world > 1 else "single process",
+            "l2": "inputs larger than L2 (0.7 GB database vs 129 MB L2), no flush"}
 
 
 def run_reference(args, rank, world):
@@ -180,32 +247,29 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    w = synth.make_workload("plain-db-scale", scale=args.scale)
-    rates = []
+    w = synth.make_workload("plain-db-scale", scale=args.scale, seed=1)
+    frac = args.ref_frac if args.ref_frac else args.cpu_frac
     for _ in range(args.warmup):
-        cpu_sample_run(w, w.queries, args.ref_frac, threads, w.total_residues, w.n_subjects)
+        cpu_sample_run(w, w.queries, frac, threads, w.total_residues * world, w.n_subjects * world)
     t_all = 0.0
     n_all = 0
     sample = None
     for _ in range(args.steps):
-        rate, dt, n_res, n_subj = cpu_sample_run(w, w.queries, args.ref_frac, threads,
-                                                 w.total_residues, w.n_subjects)
-        rates.append(rate)
+        rate, dt, n_res, n_subj, _ = cpu_sample_run(w, w.queries, frac, threads,
+                                                    w.total_residues * world, w.n_subjects * world)
         t_all += dt
         n_all += n_res
-        sample = (f"8 queries x every {int(round(1 / args.ref_frac))}th subject of the "
+        sample = (f"8 queries x every {int(round(1 / frac))}th subject of the "
                   f"{w.n_subjects}-subject database ({n_subj} subjects, "
-                  f"{n_res // 8} residues) per step")
+                  f"{n_res // 8} residues) per step, the cpu_baseline sample")
     value = n_all / t_all
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": f"synthetic (seeded; plain-db-scale workload: 8 queries, {w.n_subjects} subjects)",
-        "config": {"workload": "plain drop-in, 8 queries (100-1000 aa) vs 2M subjects / 0.7G residues",
-                   "db_subjects": w.n_subjects, "db_residues": w.total_residues,
-                   "queries": [len(q) for q in w.queries], "parallelism": "host threads",
-                   "l2": "inputs larger than L2"},
+        "data": "synthetic (seeded; 20 standard residues at Robinson-Robinson frequencies, "
+                "log-normal lengths, 1% planted homologs)",
+        "config": plain_config(w, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -215,15 +279,19 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def run_batched(args, rank, world, local):
+def batched_record(local, rank, world, scale: float, n_queries: int, warmup: int, passes: int,
+                   check_subjects: int = 5000) -> dict:
     """Batched form vs the plain path on the same queries and database
-    (batched workload: query lengths log-normal, median 350, clipped 50-2,000;
-    10% planted homologs), both timed with CUDA events."""
+    (batched workload: 512 queries, lengths log-normal, median 350, clipped
+    50-2,000; 5M subjects at scale 1; 10% planted homologs), both timed with
+    CUDA events on the search stream. Also checked: the batched HSPs equal the
+    plain path's for every query, and both equal the oracle's on every k-th
+    subject (about check_subjects of them, whole-database statistics)."""
     import blaze103
+    import oracle
     from blaze103 import synth
 
-    scale = args.scale if args.scale != 1.0 else 0.02
-    w = synth.make_workload("batched", scale=scale, n_queries=args.queries, seed=2 + 7919 * rank)
+    w = synth.make_workload("batched", scale=scale, n_queries=n_queries, seed=2 + 7919 * rank)
     db_total, db_n = w.total_residues * world, w.n_subjects * world
     db = blaze103.SeqSrc(w.residues, w.offsets, device=local)
     ps = blaze103.PrelimSearch(db)
@@ -231,85 +299,95 @@ def run_batched(args, rank, world, local):
     batch = blaze103.QueryBatch(db, w.queries)
     singles = [blaze103.Query(db, q) for q in w.queries]
     R, nq = w.total_residues, len(w.queries)
-
-    def plain_step():
-        ms = 0.0
-        for q, p in zip(singles, params):
-            ps.run_query(q, p)
-            ms += ps.stats()["device_ms"]
-        return ms
-
     last = {}
 
     def batch_step():
-        ps.run_batch(batch, params)
+        out = ps.run_batch(batch, params)
         st = ps.stats()
         last.update(st)
-        return st["device_ms"]
+        return st["device_ms"], out
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch_step()
     clocks = ClockSampler(local)
     clocks.start()
-    b_ms = [batch_step() for _ in range(args.steps)]
+    b_ms, got_b = [], None
+    for _ in range(passes):
+        ms, got_b = batch_step()
+        b_ms.append(ms)
     clk = clocks.stop()
-    plain_step()
-    p_ms = [plain_step() for _ in range(max(1, min(args.steps, 2)))]
-    b_s, p_s = sum(b_ms) / len(b_ms) / 1e3, sum(p_ms) / len(p_ms) / 1e3
-    line = {
+    p_ms, plain_lists = 0.0, []
+    for q, p in zip(singles, params):
+        ps.run_query(q, p)
+        p_ms += ps.stats()["device_ms"]
+        plain_lists.append(ps.results())
+    b_s, p_s = sum(b_ms) / len(b_ms) / 1e3, p_ms / 1e3
+
+    # batched == plain, query by query, every field
+    bounds = np.searchsorted(got_b["query"], np.arange(nq + 1))
+    same = sum(int(not np.array_equal(got_b[bounds[i]:bounds[i + 1]][list(blaze103.HSP_DTYPE.names)]
+                                      .astype(blaze103.HSP_DTYPE), plain_lists[i])) for i in range(nq))
+    # both against the oracle on a subject sample
+    k = max(w.n_subjects // max(check_subjects, 1), 1)
+    idx, res, sub_off = subject_sample(w, k)
+    ref_lists = []
+    for q in w.queries:
+        pd = oracle.default_params(len(q), db_total, db_n)
+        hs, _ = oracle.search_db(q, res, sub_off, pd, threads=os.cpu_count() or 1)
+        ref_lists.append(oracle.finish(hs, pd))
+    par = parity_check(idx, ref_lists, plain_lists, k)
+    par.update({"subjects_checked": int(len(idx)), "queries": nq, "sample": f"every {k}th subject",
+                "queries_batched_differs_from_plain": same,
+                "batched_hsps": int(len(got_b)), "plain_hsps": int(sum(len(x) for x in plain_lists))})
+    rec = {
         "metric": "DB residues/s per query, batched form (aggregate over queries)",
-        "value": nq * R / b_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": b_s * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic (seeded; batched workload: 512 queries, database scaled)",
+        "value": nq * R / b_s, "unit": UNIT, "passes": passes, "warmup": warmup,
+        "ms_per_pass": b_s * 1e3,
         "config": {"workload": f"batched: {nq} queries (log-normal median 350, 50-2000 aa) vs "
-                               f"{w.n_subjects} subjects / {R} residues, one launch per stage",
-                   "db_subjects": w.n_subjects, "db_residues": R, "queries": nq,
-                   "database_scale": scale},
-        "plain_same_workload": {"value": nq * R / p_s, "ms_per_step": p_s * 1e3},
-        "stages_ms_per_step": {"scan": last["scan_ms"], "gapped": last["gapped_ms"]},
-        "work_per_step": {k: last[k] for k in ("word_hits", "ungapped_extensions", "init_hsps",
-                                               "gapped_extensions", "dp_cells", "hsps")},
-        "dp_cells_per_s": last["dp_cells"] / (last["gapped_ms"] / 1e3) if last["gapped_ms"] else None,
+                               f"{w.n_subjects} subjects / {R} residues, 10% planted homologs",
+                   "db_subjects": w.n_subjects, "db_residues": R, "queries": nq, "database_scale": scale},
+        "plain_same_workload": {"value": nq * R / p_s, "ms_per_pass": p_s * 1e3,
+                                "form": "one search per query (scan + gapped launch sequence each)"},
         "batched_over_plain": p_s / b_s,
+        "stages_ms_per_pass": {"scan": last["scan_ms"], "gapped": last["gapped_ms"]},
+        "work_per_pass": {k_: last[k_] for k_ in ("word_hits", "ungapped_extensions", "init_hsps",
+                                                  "gapped_extensions", "dp_cells", "hsps")},
+        "dp_cells_per_s": last["dp_cells"] / (last["gapped_ms"] / 1e3) if last["gapped_ms"] else None,
+        "parity": par,
         "clocks": clk,
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     for q in singles:
         q.close()
     batch.close()
     ps.close()
     db.close()
+    return rec
 
 
-def run_serve(args, rank, world, local):
+def serve_record(local, rank, scale: float, rates, duration: float, max_queries: int, server_cfg: dict) -> dict:
     """Serving loop under Poisson arrivals (serving workload: query lengths
-    log-normal, median 350, 30-5,000; database scaled):
-    for each offered rate, queries arrive at exponential gaps, are batched on
-    the fly by the library's serving loop and completed; reports throughput
-    and p50/p99 latency (submission to completion), beside the same arrivals
+    log-normal, median 350, 30-5,000; 10M subjects at scale 1): for each
+    offered rate, queries arrive at exponential gaps, are batched on the fly
+    by the library's serving loop and completed; reports throughput and
+    p50/p99 latency (submission to completion), beside the same arrivals
     served one query at a time."""
     import blaze103
     from blaze103 import synth
 
-    scale = args.scale if args.scale != 1.0 else 0.01
     w = synth.make_workload("serving", scale=scale, seed=4 + 7919 * rank)
     rng = np.random.default_rng(44 + rank)
     pool = [synth.random_residues(rng, int(L))
             for L in synth.lognormal_lengths(rng, 512, 350, 0.82, 30, 5000)]
     db = blaze103.SeqSrc(w.residues, w.offsets, device=local)
     R = w.total_residues
-    rates = [float(x) for x in args.rates.split(",")]
 
     def serve(rate, **cfg):
         srv = blaze103.Server(db, **cfg)
-        n = max(20, min(int(rate * args.duration), args.max_queries))
+        n = max(20, min(int(rate * duration), max_queries))
         gaps = rng.exponential(1.0 / rate, n)
         picks = rng.integers(0, len(pool), n)
         tickets = []
-        t0 = time.perf_counter()
-        due = t0
+        due = time.perf_counter()
         for g, k in zip(gaps, picks):
             due += g
             d = due - time.perf_counter()
@@ -324,34 +402,55 @@ def run_serve(args, rank, world, local):
                 "residues_per_s": st["residues"] / st["busy_s"], "batches": st["batches"],
                 "p50_ms": st["latency_p50_ms"], "p99_ms": st["latency_p99_ms"], "max_ms": st["latency_max_ms"]}
 
-    batched_cfg = dict(slots=args.slots, max_batch=args.max_batch, batch_window_us=args.window_us,
-                       memory_budget=args.memory_budget)
-    serve(rates[0], **batched_cfg)  # warm-up: contexts, buffers
+    serve(rates[0], **server_cfg)  # warm-up: contexts, buffers
     clocks = ClockSampler(local)
     clocks.start()
     sweep = []
     for r in rates:
-        row = {"served": serve(r, **batched_cfg)}
+        row = {"served": serve(r, **server_cfg)}
         row["one_at_a_time"] = serve(r, slots=1, max_batch=1, batch_window_us=0)
         sweep.append(row)
     clk = clocks.stop()
+    db.close()
     top = sweep[-1]["served"]
-    line = {
+    return {
         "metric": "DB residues/s per query, served under Poisson arrivals (aggregate); p50/p99 latency",
-        "value": top["residues_per_s"], "unit": UNIT, "n_gpus": world, "steps": len(rates),
-        "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded; serving workload, database scaled)",
-        "config": {"workload": f"serving: Poisson arrivals at {args.rates} q/s, query lengths log-normal "
-                               f"(median 350, 30-5000) vs {w.n_subjects} subjects / {R} residues",
-                   "db_subjects": w.n_subjects, "db_residues": R, "database_scale": scale,
-                   "server": batched_cfg},
+        "value": top["residues_per_s"], "unit": UNIT,
+        "config": {"workload": f"serving: Poisson arrivals at {','.join(str(r) for r in rates)} q/s, query lengths "
+                               f"log-normal (median 350, 30-5000) vs {w.n_subjects} subjects / {R} residues",
+                   "db_subjects": w.n_subjects, "db_residues": R, "database_scale": scale, "server": server_cfg},
         "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
         "sweep": sweep,
         "clocks": clk,
     }
+
+
+def _standalone(rec: dict, world: int, steps: int, warmup: int) -> dict:
+    line = {"metric": rec["metric"], "value": rec["value"], "unit": UNIT, "n_gpus": world, "steps": steps,
+            "warmup": warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic (seeded)"}
+    line.update({k: v for k, v in rec.items() if k not in line})
+    return line
+
+
+def run_batched(args, rank, world, local):
+    scale = args.scale if args.scale != 1.0 else 0.02
+    rec = batched_record(local, rank, world, scale, args.queries, args.warmup, args.steps)
     if rank == 0:
-        print(json.dumps(line), flush=True)
-    db.close()
+        print(json.dumps(_standalone(rec, world, args.steps, args.warmup)), flush=True)
+
+
+def server_config(args) -> dict:
+    return dict(slots=args.slots, max_batch=args.max_batch, batch_window_us=args.window_us,
+                memory_budget=args.memory_budget)
+
+
+def run_serve(args, rank, world, local):
+    scale = args.scale if args.scale != 1.0 else 0.01
+    rates = [float(x) for x in args.rates.split(",")]
+    rec = serve_record(local, rank, scale, rates, args.duration, args.max_queries, server_config(args))
+    if rank == 0:
+        print(json.dumps(_standalone(rec, world, len(rates), 1)), flush=True)
 
 
 def main():
@@ -362,8 +461,16 @@ def main():
     ap.add_argument("--impl", default="blaze", choices=["blaze", "reference"])
     ap.add_argument("--scale", type=float, default=1.0, help="database size relative to the default workload (2M subjects)")
     ap.add_argument("--cpu-frac", type=float, default=0.25, help="cpu_baseline sample fraction")
-    ap.add_argument("--ref-frac", type=float, default=0.02, help="reference arm sample fraction per step")
+    ap.add_argument("--ref-frac", type=float, default=None,
+                    help="reference arm sample fraction per step (default: the cpu_baseline fraction)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="plain line without its batched sub-record")
+    ap.add_argument("--no-serve", action="store_true", help="plain line without its serving sub-record")
+    ap.add_argument("--batched-scale", type=float, default=1.0,
+                    help="batched sub-record: database size relative to 5M subjects")
+    ap.add_argument("--serve-scale", type=float, default=0.1,
+                    help="serving sub-record: database size relative to 10M subjects")
+    ap.add_argument("--serve-rates", default="20,100,400", help="serving sub-record: arrival rates, queries/s")
     ap.add_argument("--mode", default="plain", choices=["plain", "batched", "serve"],
                     help="plain: the drop-in, one query per launch sequence (the headline line); "
                          "batched: many queries per launch against a 5M-subject-shaped database, scaled")
@@ -437,11 +544,12 @@ def main():
         for q, p in zip(w.queries, params):
             ps.prelim_search(q, p, cap)
     h2d = d2h = 0
+    e2e_out = [None] * len(w.queries)
     group.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for q, p in zip(w.queries, params):
-            ps.prelim_search(q, p, cap)
+        for i, (q, p) in enumerate(zip(w.queries, params)):
+            e2e_out[i] = ps.prelim_search(q, p, cap)
             st = ps.stats()
             h2d += st["h2d_bytes"]
             d2h += st["d2h_bytes"]
@@ -486,11 +594,8 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded; 20 standard residues at Robinson-Robinson frequencies, "
                 "log-normal lengths, 1% planted homologs)",
-        "config": {"workload": "plain drop-in, 8 queries (100-1000 aa) vs 2M subjects / 0.7G residues "
-                               "resident in HBM, one launch sequence per query",
-                   "db_subjects": N, "db_residues": R, "queries": [len(q) for q in w.queries],
-                   "parallelism": f"weak x{world} (one database per rank)" if world > 1 else "1 GPU",
-                   "l2": "inputs larger than L2 (0.7 GB database vs 129 MB L2), no flush"},
+        "config": plain_config(w, world),
+        "placement": "database and query tables resident in HBM; one scan + gapped launch sequence per query",
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
                 "path": "blaze_prelim_search with host query and result buffers"},
@@ -511,18 +616,33 @@ def main():
     }
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, dt, n_res, n_subj = cpu_sample_run(w, w.queries, args.cpu_frac, threads, db_total, db_n)
+        rate, dt, n_res, n_subj, sample = cpu_sample_run(w, w.queries, args.cpu_frac, threads, db_total, db_n,
+                                                         keep=True)
+        k = max(int(round(1.0 / args.cpu_frac)), 1)
         line["cpu_baseline"] = {
             "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"8 queries x every {int(round(1 / args.cpu_frac))}th subject "
+            "sample": f"8 queries x every {k}th subject "
                       f"({n_subj} subjects, {n_res // 8} residues), {dt:.1f} s",
         }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+        # the oracle's HSPs of that sample against the e2e path's, same OIDs
+        par = parity_check(sample[0], sample[1], e2e_out, k)
+        par.update({"subjects_checked": n_subj, "queries": len(w.queries),
+                    "sample": f"every {k}th subject, whole-database statistics",
+                    "path": "e2e (blaze_prelim_search)", "oracle": "oracle/blaze_oracle.c"})
+        line["parity"] = par
     for q in queries:
         q.close()
     ps.close()
     db.close()
+    # sub-records (N=1 only): the batched form and the serving loop
+    if world == 1 and not args.no_batched:
+        line["batched"] = batched_record(local, rank, world, args.batched_scale, args.queries, 1, 1)
+    if world == 1 and not args.no_serve:
+        rates = [float(x) for x in args.serve_rates.split(",")]
+        line["serve"] = serve_record(local, rank, args.serve_scale, rates, args.duration, args.max_queries,
+                                     server_config(args))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     group.close()
 
 

@@ -71,6 +71,53 @@ class SeqSrc:
         self._adopt(h, device)
         return self
 
+    @classmethod
+    def from_source(cls, source, device: int = 0) -> "SeqSrc":
+        """The resident database read from a BlastSeqSrc-shaped source
+        (blaze_db_create_from_source). `source` provides ``num_seqs()`` and
+        ``get_sequence(oid)`` (NCBIstdaa codes as a uint8 array), and may
+        provide ``seq_len(oid)``, ``release_sequence(oid)``, ``tot_len()``,
+        ``max_seq_len()`` and ``iter_next()`` (the next OID, negative at the
+        end) -- the accessors of NCBI's BlastSeqSrc
+        (BLAZE_ncbi/blast_seqsrc.c:91-130)."""
+        from ._lib import (GET_INT64_FN, GET_NUM_SEQS_FN, GET_SEQ_LEN_FN, GET_SEQUENCE_FN, RELEASE_SEQUENCE_FN,
+                           BlazeSeqSource)
+
+        held = {}  # oid -> array kept alive until its release
+
+        def get_sequence(_u, oid, res_out, len_out):
+            try:
+                a = np.ascontiguousarray(source.get_sequence(int(oid)), dtype=np.uint8)
+            except Exception:
+                return 1
+            held[int(oid)] = a
+            res_out[0] = a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+            len_out[0] = a.size
+            return 0
+
+        def release(_u, oid):
+            held.pop(int(oid), None)
+            if hasattr(source, "release_sequence"):
+                source.release_sequence(int(oid))
+
+        def opt(name, ftype, fn):
+            return ftype(fn) if hasattr(source, name) else ctypes.cast(None, ftype)
+
+        cbs = BlazeSeqSource(
+            None, GET_NUM_SEQS_FN(lambda _u: int(source.num_seqs())), GET_SEQUENCE_FN(get_sequence),
+            RELEASE_SEQUENCE_FN(release),
+            opt("seq_len", GET_SEQ_LEN_FN, lambda _u, oid: int(source.seq_len(int(oid)))),
+            opt("tot_len", GET_INT64_FN, lambda _u: int(source.tot_len())),
+            opt("max_seq_len", GET_INT64_FN, lambda _u: int(source.max_seq_len())),
+            opt("iter_next", GET_INT64_FN, lambda _u: int(source.iter_next())))
+        self = cls.__new__(cls)
+        self._lib = load()
+        h = ctypes.c_void_p()
+        check(self._lib.blaze_db_create_from_source(int(device), ctypes.byref(cbs), ctypes.byref(h)),
+              "blaze_db_create_from_source")
+        self._adopt(h, device)
+        return self
+
     def _adopt(self, h, device):
         self._h = h
         self.device = device

@@ -21,7 +21,7 @@ EXPORTS = (
     "blaze_server_create", "blaze_server_submit", "blaze_server_wait", "blaze_server_take",
     "blaze_server_stats_get", "blaze_server_free", "blaze_volume_info", "blaze_volume_read", "blaze_db_open",
     "blaze_search_traceback", "blaze_search_traceback_results", "blaze_search_traceback_batch",
-    "blaze_search_traceback_batch_results",
+    "blaze_search_traceback_batch_results", "blaze_db_create_from_source",
 )
 
 HSP_DTYPE = np.dtype([
@@ -105,6 +105,23 @@ class BlazeServerStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+# Callback types of blaze_seq_source (the BlastSeqSrc-shaped database source).
+GET_NUM_SEQS_FN = ctypes.CFUNCTYPE(ctypes.c_int64, ctypes.c_void_p)
+GET_SEQUENCE_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32,
+                                   ctypes.POINTER(ctypes.POINTER(ctypes.c_uint8)), ctypes.POINTER(ctypes.c_uint32))
+RELEASE_SEQUENCE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint32)
+GET_SEQ_LEN_FN = ctypes.CFUNCTYPE(ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint32)
+GET_INT64_FN = ctypes.CFUNCTYPE(ctypes.c_int64, ctypes.c_void_p)
+
+
+class BlazeSeqSource(ctypes.Structure):
+    _fields_ = [
+        ("user", ctypes.c_void_p), ("get_num_seqs", GET_NUM_SEQS_FN), ("get_sequence", GET_SEQUENCE_FN),
+        ("release_sequence", RELEASE_SEQUENCE_FN), ("get_seq_len", GET_SEQ_LEN_FN),
+        ("get_tot_len", GET_INT64_FN), ("get_max_seq_len", GET_INT64_FN), ("iter_next", GET_INT64_FN),
+    ]
+
+
 class BlazeError(RuntimeError):
     def __init__(self, status: int, what: str):
         self.status = status
@@ -173,6 +190,7 @@ def load(path: str | None = None):
     L.blaze_search_traceback_results.argtypes = [vp, vp, ctypes.c_uint64, u64p]
     L.blaze_search_traceback_batch.argtypes = [vp, vp, ctypes.POINTER(BlazeParams), i32, ctypes.c_double, u64p]
     L.blaze_search_traceback_batch_results.argtypes = [vp, vp, ctypes.c_uint64, u64p]
+    L.blaze_db_create_from_source.argtypes = [ctypes.c_int, ctypes.POINTER(BlazeSeqSource), ctypes.POINTER(vp)]
     for name in EXPORTS:
         if name not in ("blaze_status_string", "blaze_last_cuda_error"):
             getattr(L, name).restype = ctypes.c_int

@@ -28,6 +28,7 @@ RR_FREQS = RR_FREQS / RR_FREQS.sum()
 UNGAPPED_LAMBDA = 0.3176
 
 _TABLE_BITS = 16
+HOMOLOG_POOL = 100_000  # distinct mutants at most per database (see make_workload)
 
 
 def _sampling_table() -> np.ndarray:
@@ -165,15 +166,23 @@ def make_workload(workload, scale: float = 1.0, seed: int | None = None,
         letters = rng.choice(STD_CODES, size=3, replace=False)
         pos = int(offsets[i]) + int(rng.integers(0, L - run + 1))
         residues[pos:pos + run] = letters[rng.integers(0, 3, size=run)]
-    # planted homologs
+    # planted homologs; above kHomologPool of them (full-size databases with
+    # many homologs), each planted subject takes a mutant drawn from a pool
+    # of kHomologPool independently made ones, so building a 500,000-homolog
+    # database stays a matter of seconds
     n_h = int(round(c["homolog_frac"] * n))
     planted = np.sort(rng.choice(n, size=n_h, replace=False)) if n_h else np.zeros(0, np.int64)
     id_lo, id_hi = c["identity"]
-    for i in planted:
+
+    def one_mutant():
         q = queries[int(rng.integers(0, len(queries)))]
         w = int(min(rng.integers(100, 301), len(q)))
         qs = int(rng.integers(0, len(q) - w + 1))
-        hom = mutate(rng, q[qs:qs + w], float(rng.uniform(id_lo, id_hi)))
+        return mutate(rng, q[qs:qs + w], float(rng.uniform(id_lo, id_hi)))
+
+    pool = [one_mutant() for _ in range(HOMOLOG_POOL)] if n_h > HOMOLOG_POOL else None
+    for i in planted:
+        hom = pool[int(rng.integers(0, HOMOLOG_POOL))] if pool is not None else one_mutant()
         L = int(lengths[i])
         hom = hom[:L]
         pos = int(offsets[i]) + int(rng.integers(0, L - len(hom) + 1))

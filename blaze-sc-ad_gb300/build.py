@@ -18,7 +18,7 @@ INCLUDE = os.path.join(REPO, "include")
 OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "blaze103", "libblaze103.so")
 SOURCES = ["scan.cu", "kernels.cu", "traceback.cu", "api.cu", "batch.cu", "traceback_host.cu", "host.cpp",
-           "noalloc.cu", "server.cpp", "volume.cpp"]
+           "noalloc.cu", "server.cpp", "volume.cpp", "seqsrc.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

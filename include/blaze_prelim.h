@@ -139,6 +139,45 @@ int blaze_db_free(blaze_db *db);
 int blaze_db_info(const blaze_db *db, uint64_t *total_residues, uint32_t *n_subjects,
                   uint32_t *max_length);
 
+/* A database source shaped like NCBI's BlastSeqSrc, so that an engine that
+ * already holds a BlastSeqSrc* hands it over through a thin adapter
+ * (function pointers plus a user pointer; BLAZE_ncbi/blast_seqsrc.c:91-130 and
+ * the accessors BlastSeqSrcGetNumSeqs, GetTotLen, GetMaxSeqLen, GetSeqLen,
+ * GetSequence :325-333, ReleaseSequence, IteratorNext). It replaces the
+ * reference GPU driver's per-chunk gathers through BlastSeqSrcGetSequence
+ * (BLAZE_gpu/gpuBLAZE.cu:1587-1611): the library reads every sequence once,
+ * on the calling thread, into its resident length-sorted copy.
+ *
+ *   get_num_seqs      number of OIDs (>= 0); required
+ *   get_sequence      residues of `oid` (NCBIstdaa codes 1..27, no sentinel
+ *                     bytes) and their count; the pointer stays valid until
+ *                     release_sequence(oid) or the next get_sequence; returns
+ *                     0 on success; required
+ *   release_sequence  called after each get_sequence (may be NULL)
+ *   get_seq_len       length of `oid` without fetching it (may be NULL: the
+ *                     lengths are then taken from a first get_sequence pass)
+ *   get_tot_len, get_max_seq_len
+ *                     may be NULL; when given (and iter_next is NULL), they
+ *                     must equal the total and the largest length read
+ *   iter_next         the next OID to search, negative at the end (NCBI's
+ *                     BLAST_SEQSRC_EOF); may be NULL: every OID. OIDs the
+ *                     iterator does not return stay in the database as empty
+ *                     subjects, so OID numbering is kept.
+ * A callback error, a length that disagrees between calls, an OID out of
+ * range or returned twice by iter_next, a residue code outside 1..27 or
+ * totals that disagree return BLAZE_ERR_INVALID_ARG and create nothing. */
+typedef struct blaze_seq_source {
+    void *user;
+    int64_t (*get_num_seqs)(void *user);
+    int (*get_sequence)(void *user, uint32_t oid, const uint8_t **residues, uint32_t *length);
+    void (*release_sequence)(void *user, uint32_t oid);
+    int64_t (*get_seq_len)(void *user, uint32_t oid);
+    int64_t (*get_tot_len)(void *user);
+    int64_t (*get_max_seq_len)(void *user);
+    int64_t (*iter_next)(void *user);
+} blaze_seq_source;
+int blaze_db_create_from_source(int device, const blaze_seq_source *src, blaze_db **out);
+
 /* NCBI BLAST protein database volume: `path` without extension names the
  * <path>.pin index and <path>.psq sequence file (format versions 4 and 5).
  * OID i of the volume becomes subject i. Replaces the per-subject

@@ -106,7 +106,7 @@ int main(void) {
                    (void *)blaze_server_submit, (void *)blaze_server_wait, (void *)blaze_server_take,
                    (void *)blaze_server_stats_get, (void *)blaze_server_free, (void *)blaze_volume_info,
                    (void *)blaze_volume_read, (void *)blaze_db_open, (void *)blaze_gapped_noalloc,
-                   (void *)blaze_last_cuda_error};
+                   (void *)blaze_last_cuda_error, (void *)blaze_db_create_from_source};
     return fns[0] == 0;
 }
 """
@@ -132,3 +132,34 @@ def test_header_compiles_and_links_from_c(lib, tmp_path):
     o = oracle.default_params(300, 7_000_000, 20_000)
     assert [int(x) for x in out[:5]] == [o["gapped_cutoff"], o["ungapped_cutoff"], 40, 38, 0]
     assert "output" in " ".join(out[5:])
+
+
+def build_c_client(name: str, out_dir) -> str:
+    """Compiles tests/clients/<name>.c as C99 against the public header and
+    links it to libblaze103."""
+    import shutil
+    import subprocess
+
+    import blaze103
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    exe = os.path.join(str(out_dir), name)
+    libdir = os.path.dirname(blaze103._lib.LIB_PATH)
+    cmd = ["gcc", "-std=c99", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "clients", name + ".c"), "-L", libdir, "-lblaze103",
+           f"-Wl,-rpath,{libdir}", "-o", exe]
+    subprocess.run(cmd, check=True, capture_output=True)
+    return exe
+
+
+def test_seq_source_client_builds_and_reports_no_device(lib, tmp_path):
+    import subprocess
+
+    import blaze103
+
+    exe = build_c_client("seqsrc_client", tmp_path)
+    if blaze103.device_count() > 0:
+        pytest.skip("a GPU is present: tests/test_gpu_seqsrc.py runs the client")
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "status 3", r.stdout
