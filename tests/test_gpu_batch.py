@@ -175,3 +175,45 @@ def test_batch_culling_per_query():
     batch.close()
     ps.close()
     db.close()
+
+
+def test_config2_batched_against_oracle_on_a_subject_sample():
+    # the batched workload's 512 queries (log-normal, median 350, 50-2,000)
+    # against a 5% slice of its 5M-subject database (10% planted homologs):
+    # every query's batched HSPs on every 50th subject equal the oracle's,
+    # under the statistics of the whole slice
+    import os
+
+    import oracle
+
+    w = synth.make_workload("batched", scale=0.05)
+    assert len(w.queries) == 512
+    db = blaze103.SeqSrc(w.residues, w.offsets)
+    ps = blaze103.PrelimSearch(db)
+    params = [params_for(len(q), db.tot_len, db.num_seqs)[0] for q in w.queries]
+    batch = blaze103.QueryBatch(db, w.queries)
+    got = ps.run_batch(batch, params)
+    k = 50
+    idx = np.arange(0, w.n_subjects, k)
+    sres = np.concatenate([w.residues[int(w.offsets[i]):int(w.offsets[i + 1])] for i in idx])
+    soff = np.zeros(len(idx) + 1, dtype=np.uint64)
+    np.cumsum((w.offsets[idx + 1] - w.offsets[idx]).astype(np.int64), out=soff[1:])
+    bounds = np.searchsorted(got["query"], np.arange(len(w.queries) + 1))
+    checked = 0
+    for i, q in enumerate(w.queries):
+        pd = params_for(len(q), db.tot_len, db.num_seqs)[1]
+        hs, _ = oracle.search_db(q, sres, soff, pd, threads=os.cpu_count() or 1)
+        ref = oracle.finish(hs, pd)
+        g = got[bounds[i]:bounds[i + 1]]
+        g = g[(g["oid"] % k) == 0]
+        assert np.array_equal(g["oid"], idx[ref["subject"]].astype(np.uint32)), i
+        for f in ("score", "q_start", "q_end", "s_start", "s_end"):
+            assert np.array_equal(g[f], ref[f]), (i, f)
+        assert np.array_equal(g["q_gapped_start"], ref["q_gstart"]), i
+        assert np.array_equal(g["s_gapped_start"], ref["s_gstart"]), i
+        assert np.allclose(g["evalue"], ref["evalue"], rtol=1e-12, atol=0.0), i
+        checked += len(ref)
+    assert checked > 500
+    batch.close()
+    ps.close()
+    db.close()

@@ -14,11 +14,56 @@ from _parity import compare, concat, params_for
 pytestmark = pytest.mark.gpu
 
 
-def test_config0_scaled():
-    w = synth.make_workload("plain-small", scale=0.25)
+def test_config0_full_size():
+    # the plain small workload at its stated size: 1 query of 300 residues,
+    # 20,000 subjects (~7M residues), 1% planted homologs
+    w = synth.make_workload("plain-small", scale=1.0)
+    assert w.n_subjects == 20_000
     got, ref, stats = compare(w.queries[0], w.residues, w.offsets)
-    assert len(got) > 0 and stats["dp_cells"] > 0
+    assert len(got) > 100 and stats["dp_cells"] > 0
     assert np.isin(w.planted, got["oid"]).mean() > 0.9
+
+
+def test_config1_queries_on_a_database_slice():
+    # the eight database-scale queries (100-1,000 residues) against a 2%
+    # slice of that database's shape (40,000 subjects)
+    w = synth.make_workload("plain-db-scale", scale=0.02)
+    for q in w.queries:
+        compare(q, w.residues, w.offsets)
+
+
+def test_config3_slice_long_queries_long_and_low_complexity_subjects():
+    # the overflow-stress workload's own queries (2,000-5,000 residues)
+    # against a slice with its longest subjects (up to 35,000 residues) and
+    # its low-complexity runs: 3-letter stretches in 20% of subjects
+    # (a 20% database's 2,000 longest subjects plus 3,000 others, and three
+    # subjects at the workload's length bound -- 20,000, 30,000 and 35,000
+    # residues -- each with homologs of the queries and low-complexity runs)
+    w = synth.make_workload("overflow-stress", scale=0.2, n_queries=3)
+    rng = np.random.default_rng(33)
+    pick = np.concatenate([np.arange(w.n_subjects - 2000, w.n_subjects),
+                           rng.choice(w.n_subjects - 2000, size=3000, replace=False)])
+    pick.sort()
+    seqs = [w.residues[int(w.offsets[i]):int(w.offsets[i + 1])] for i in pick]
+    alpha = np.array([1, 11, 17], dtype=np.uint8)
+    for L in (20_000, 30_000, 35_000):
+        s = synth.random_residues(rng, L)
+        for k, q in enumerate(w.queries):
+            hom = synth.mutate(rng, q[100 * k:100 * k + 600], 0.45)
+            p = int(rng.integers(0, L - len(hom)))
+            s[p:p + len(hom)] = hom
+        for _ in range(6):
+            p = int(rng.integers(0, L - 200))
+            s[p:p + 150] = alpha[rng.integers(0, 3, 150)]
+        seqs.append(s)
+    res, off = concat(seqs)
+    assert int(np.diff(off.astype(np.int64)).max()) == 35_000 and min(len(q) for q in w.queries) >= 2000
+    runs = 0
+    for q in w.queries:
+        got, _, stats = compare(q, res, off)
+        assert len(got) > 0
+        runs += stats["ungapped_extensions"]
+    assert runs > 10_000
 
 
 @pytest.mark.parametrize("qlen", [3, 11, 64, 100, 300, 1000, 2500])
