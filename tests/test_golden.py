@@ -7,7 +7,10 @@ import numpy as np
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+# the oracle's regression fixtures (ref_lookup.npz holds vectors made by the
+# reference's own code: tests/test_ref_lookup.py)
+FIXTURES = sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
+                  if os.path.basename(p) != "ref_lookup.npz")
 PARAM_KEYS = ["word_threshold", "window", "ungapped_xdrop", "ungapped_cutoff", "gap_open",
               "gap_extend", "gapped_xdrop", "gapped_cutoff"]
 
