@@ -487,7 +487,9 @@ static int run_pass(blaze_search *s, const RunSpec &r, const std::vector<ScanPla
     if ((rc = s->groups.ensure(s->out_cap)) != BLAZE_OK) return rc;  // a published list holds >= 1 HSP
     if ((rc = s->qkept.ensure(nq)) != BLAZE_OK) return rc;
     if (batched && (rc = s->work_query.ensure(work_cap)) != BLAZE_OK) return rc;
-    const size_t dp_stride = static_cast<size_t>(std::max<uint32_t>(db->max_len, 1)) + 2;
+    // DP rows of the longest subject plus 2, even so that each warp's H and E
+    // rows start 8-byte aligned (the DP reads and writes column pairs)
+    const size_t dp_stride = (static_cast<size_t>(std::max<uint32_t>(db->max_len, 1)) + 3) & ~size_t{1};
     if ((rc = s->dp.ensure(gapped_warps * 2 * dp_stride)) != BLAZE_OK) return rc;
     if ((rc = s->cursors.ensure(plans.size())) != BLAZE_OK) return rc;
 

@@ -151,8 +151,8 @@ struct GappedArgs {
     InitHit *sorted;     // per warp: cap records
     DevHsp *saved;       // per warp: cap records
     uint32_t cap;
-    int32_t *dp;         // per warp: 2 * dp_stride ints
-    uint32_t dp_stride;  // >= max subject length + 2
+    int32_t *dp;         // per warp: 2 * dp_stride ints, 8-byte aligned
+    uint32_t dp_stride;  // >= max subject length + 2, even
     int32_t gap_open, gap_extend, xdrop, cutoff;
     int32_t smin, max_hsps;  // single query: as batch_smin / batch_max_hsps
     DevHsp *out;

@@ -61,17 +61,20 @@ __device__ int32_t gapped_start(const uint8_t *q, const uint8_t *s, int32_t q_st
 }
 
 // Score-only X-drop DP from the origin, computed one row at a time with the
-// 32 lanes spread over the row's live columns. Row a, column b scores the
-// a-th row letter against the b-th column letter (REV: both read backwards
-// from the ends of A and B). Within a row the row-gap term and the running
-// best are prefix maxima; a cell is live when it is within xdrop of the best
-// seen so far in row-major order. Cells below that bound can never become
-// live again, so computing the prefix maxima over every cell of the band
-// (live or not) leaves all live values and the live set exactly those of the
-// sequential band algorithm the oracle runs. The running best's prefix
-// maximum is taken only in a 32-column step whose largest value beats the
-// best carried into it (a warp max-reduce decides); in every other step the
-// carried best is each cell's best so far.
+// warp spread over the row's live columns, two adjacent columns per lane (64
+// per step: most rows of a band are 33 to 64 wide, so a row is one step).
+// Row a, column b scores the a-th row letter against the b-th column letter
+// (REV: both read backwards from the ends of A and B). Within a row the
+// row-gap term and the running best are prefix maxima (within the lane's
+// pair, then across lanes); a cell is live when it is within xdrop of the
+// best seen so far in row-major order. Cells below that bound can never
+// become live again, so computing the prefix maxima over every cell of the
+// band (live or not) leaves all live values and the live set exactly those
+// of the sequential band algorithm the oracle runs. The running best's prefix
+// maximum is taken only in a step whose largest value beats the best carried
+// into it (a warp max-reduce decides); in every other step the carried best
+// is each cell's best so far. Hb and Eb are 8-byte aligned and hold at least
+// N + 2 entries, so the pair loads and stores of a live column stay inside.
 template <bool REV>
 __device__ int32_t xdrop_dp(const uint8_t *__restrict__ A, const uint8_t *__restrict__ B, int32_t M,
                             int32_t N, int32_t gap_open, int32_t gap_extend, int32_t xdrop,
@@ -96,62 +99,79 @@ __device__ int32_t xdrop_dp(const uint8_t *__restrict__ A, const uint8_t *__rest
         int32_t carry_p = kNeg, carry_best = best, carry_hold = kNeg;
         int32_t first_alive = -1, last_alive = -1, row_best = best, row_best_b = -1;
         *cells += static_cast<unsigned long long>(bsize - first);
-        for (int32_t c0 = first; c0 < bsize; c0 += 32) {
-            const int32_t b = c0 + lane;
-            const bool act = b < bsize;
-            const int32_t hold = act ? Hb[b] : kNeg;
-            const int32_t ein = act ? Eb[b] : kNeg;
-            int32_t hprev = __shfl_up_sync(kFull, hold, 1);
-            if (lane == 0) hprev = carry_hold;
-            int32_t D = ein;
-            if (act && b > first) D = max(D, hprev + row[REV ? B[N - b] : B[b]]);
-            const int32_t P = act ? max(D, kNeg) + ge * b : kNeg;
-            int32_t incl = P;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int32_t x = __shfl_up_sync(kFull, incl, o);
-                if (lane >= o) incl = max(incl, x);
+        for (int32_t c0 = first & ~1; c0 < bsize; c0 += 64) {
+            const int32_t b0 = c0 + 2 * lane, b1 = b0 + 1;
+            const bool act0 = b0 >= first && b0 < bsize, act1 = b1 >= first && b1 < bsize;
+            int2 hold = make_int2(kNeg, kNeg), ein = make_int2(kNeg, kNeg);
+            if (b0 < bsize) {  // b1 <= bsize <= N + 1: inside the rows
+                hold = *reinterpret_cast<const int2 *>(Hb + b0);
+                ein = *reinterpret_cast<const int2 *>(Eb + b0);
             }
+            if (!act0) hold.x = ein.x = kNeg;
+            if (!act1) hold.y = ein.y = kNeg;
+            int32_t hprev = __shfl_up_sync(kFull, hold.y, 1);
+            if (lane == 0) hprev = carry_hold;
+            int32_t D0 = ein.x, D1 = ein.y;
+            if (act0 && b0 > first) D0 = __viaddmax_s32(hprev, row[REV ? B[N - b0] : B[b0]], D0);
+            if (act1 && b1 > first) D1 = __viaddmax_s32(hold.x, row[REV ? B[N - b1] : B[b1]], D1);
+            const int32_t P0 = act0 ? max(D0, kNeg) + ge * b0 : kNeg;
+            const int32_t P1 = act1 ? max(D1, kNeg) + ge * b1 : kNeg;
+            // row gap: prefix maximum of P over the columns before each cell
+            int32_t incl = max(P0, P1);
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) incl = max(incl, __shfl_up_sync(kFull, incl, o));  // lanes < o get their own
             int32_t excl = __shfl_up_sync(kFull, incl, 1);
             if (lane == 0) excl = kNeg;
             excl = max(excl, carry_p);
-            const int32_t G = excl - goe + ge - ge * b;
-            const int32_t H = max(D, G);
-            // the best so far in row-major order: only a segment whose largest
+            const int32_t G0 = excl - goe + ge - ge * b0;
+            const int32_t G1 = max(excl, P0) - goe + ge - ge * b1;
+            const int32_t H0 = max(D0, G0), H1 = max(D1, G1);
+            // the best so far in row-major order: only a step whose largest
             // H beats the carried best needs the prefix maximum
-            const int32_t hv = act ? H : INT32_MIN;
-            const int32_t cm = __reduce_max_sync(kFull, hv);
-            int32_t cur_best = carry_best;
+            const int32_t hv0 = act0 ? H0 : INT32_MIN, hv1 = act1 ? H1 : INT32_MIN;
+            const int32_t cm = __reduce_max_sync(kFull, max(hv0, hv1));
+            int32_t best0 = carry_best, best1 = carry_best;
             if (cm > carry_best) {
-                int32_t inclh = hv;
+                int32_t inclh = max(hv0, hv1);
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int32_t x = __shfl_up_sync(kFull, inclh, o);
-                    if (lane >= o) inclh = max(inclh, x);
-                }
+                for (int o = 1; o < 32; o <<= 1) inclh = max(inclh, __shfl_up_sync(kFull, inclh, o));
                 int32_t exclh = __shfl_up_sync(kFull, inclh, 1);
                 if (lane == 0) exclh = INT32_MIN;
-                cur_best = max(carry_best, exclh);
-                const unsigned mm = __ballot_sync(kFull, act && H == cm);
+                best0 = max(carry_best, exclh);
+                best1 = max(best0, hv0);
+                const unsigned m0 = __ballot_sync(kFull, act0 && H0 == cm);
+                const unsigned m1 = __ballot_sync(kFull, act1 && H1 == cm);
+                const int f0 = m0 ? 2 * (__ffs(m0) - 1) : 64, f1 = m1 ? 2 * (__ffs(m1) - 1) + 1 : 64;
                 row_best = cm;
-                row_best_b = c0 + __ffs(mm) - 1;
+                row_best_b = c0 + min(f0, f1);
                 carry_best = cm;
             }
-            const bool alive = act && (cur_best - H <= xdrop);
-            const unsigned am = __ballot_sync(kFull, alive);
-            if (am) {
-                if (first_alive < 0) first_alive = c0 + __ffs(am) - 1;
-                last_alive = c0 + 31 - __clz(am);
+            const bool alive0 = act0 && (best0 - H0 <= xdrop);
+            const bool alive1 = act1 && (best1 - H1 <= xdrop);
+            const unsigned a0 = __ballot_sync(kFull, alive0), a1 = __ballot_sync(kFull, alive1);
+            if (a0 | a1) {
+                const int f0 = a0 ? 2 * (__ffs(a0) - 1) : 64, f1 = a1 ? 2 * (__ffs(a1) - 1) + 1 : 64;
+                const int l0 = a0 ? 2 * (31 - __clz(a0)) : -1, l1 = a1 ? 2 * (31 - __clz(a1)) + 1 : -1;
+                if (first_alive < 0) first_alive = c0 + min(f0, f1);
+                last_alive = c0 + max(l0, l1);
             }
-            carry_hold = __shfl_sync(kFull, hold, 31);
+            carry_hold = __shfl_sync(kFull, hold.y, 31);
             carry_p = max(carry_p, __shfl_sync(kFull, incl, 31));
             __syncwarp();
-            if (act) {
-                if (alive) {
-                    Eb[b] = max(H - goe, ein - ge);
-                    Hb[b] = H;
-                } else if (first_alive >= 0 && b > first_alive) {
-                    Hb[b] = kNeg;
+            if (act0) {
+                if (alive0) {
+                    Eb[b0] = __viaddmax_s32(H0, -goe, ein.x - ge);
+                    Hb[b0] = H0;
+                } else if (first_alive >= 0 && b0 > first_alive) {
+                    Hb[b0] = kNeg;
+                }
+            }
+            if (act1) {
+                if (alive1) {
+                    Eb[b1] = __viaddmax_s32(H1, -goe, ein.y - ge);
+                    Hb[b1] = H1;
+                } else if (first_alive >= 0 && b1 > first_alive) {
+                    Hb[b1] = kNeg;
                 }
             }
             __syncwarp();
