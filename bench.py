@@ -587,6 +587,32 @@ def main():
         except (OSError, ValueError, KeyError, ZeroDivisionError):
             traffic = None
 
+    # the scan's real bound: integer issue. Warp instructions per step from
+    # the committed ncu count (scaled by residues), against the SMs' issue
+    # rate (4 schedulers per SM, one warp instruction per cycle each, at the
+    # maximum SM clock)
+    issue = None
+    iprof = os.path.join(ROOT, "profiles", "scan_kernel_issue.json")
+    if os.path.exists(iprof):
+        try:
+            import torch
+
+            with open(iprof) as f:
+                ij = json.load(f)
+            if [x["query_length"] for x in ij["per_query"]] == [len(q) for q in w.queries]:
+                inst = ij["warp_inst_per_step"] * R / ij["captured_residues"]
+                n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+                mhz = clk.get("sm_max_mhz") or 2070.0
+                peak_rate = n_sm * 4 * mhz * 1e6
+                rate = inst / (acc["scan_ms"] / 1e3 / args.steps)
+                issue = {"kernel": "scan_kernel", "warp_inst_per_step": inst,
+                         "warp_inst_per_residue": inst / (R * len(queries)),
+                         "achieved_warp_inst_per_s": rate, "peak_warp_inst_per_s": peak_rate,
+                         "frac": rate / peak_rate,
+                         "source": "profiles/scan_kernel_issue.json (ncu sm__inst_executed.sum, scaled by residues)"}
+        except (OSError, ValueError, KeyError, ImportError, RuntimeError):
+            issue = None
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
@@ -604,6 +630,7 @@ def main():
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
                      "kernel": "scan_kernel", "alg_bytes_per_launch": alg_bytes,
                      "avg_launch_ms": scan_avg_s * 1e3},
+        "issue_roofline": issue,
         "stages_ms_per_step": {"scan": acc["scan_ms"] / args.steps,
                                "gapped": acc["gapped_ms"] / args.steps},
         "dp_cells_per_s": acc["dp_cells"] / (acc["gapped_ms"] / 1e3) if acc["gapped_ms"] else None,

@@ -3,10 +3,11 @@
 For each named shape (a query-length profile, a batch size and a database
 size) it times the search over a grid of launch settings with CUDA events --
 the subject staging bound (subjects up to `stage_bytes` residues are staged in
-shared memory, longer ones are read from global memory), warps per scan block
-and residues per batched tile -- checks that every setting returns the same
-HSPs, and writes the fastest setting per shape to ``tuning.json`` beside this
-file. ``lookup`` returns the entry of the nearest shape; ``PrelimSearch``
+shared memory, longer ones are read from global memory), warps per scan block,
+residues per batched tile and the batched launch mode (tiles of many queries
+per launch, or one launch per query) -- checks that every setting returns the
+same HSPs, and writes the fastest setting per shape to ``tuning.json`` beside
+this file. ``lookup`` returns the entry of the nearest shape; ``PrelimSearch``
 applies it to batched runs unless a tuning was set explicitly.
 
 Run on the GPU:  python blaze-sc-ad_gb300/blaze103/autotune.py [--quick]
@@ -26,19 +27,27 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 TUNING_PATH = os.path.join(HERE, "tuning.json")
 
-# shapes: (kind, synthetic workload, scale of its database, queries)
+# shapes: (kind, synthetic workload, scale of its database, queries, grid,
+# timed repetitions). Knobs: the subject staging bound, warps per scan block
+# (0: as many as registers allow), residues per warp of a batched tile (0:
+# several tiles' worth per warp) and the batched launch mode (1: tiles of
+# many queries per launch, 2: one scan launch per query).
+_SMALL_BATCH_GRID = {
+    "stage_bytes": (1024, 2048),
+    "max_warps_per_block": (16, 0),
+    "tile_residues": (0, 4096, 65536),
+    "batch_launch": (1, 2),
+}
 SHAPES = {
-    "plain-db-scale": ("plain", "plain-db-scale", 0.1, 8),
-    "batched-512": ("batched", "batched", 0.02, 512),
-    "batched-64": ("batched", "batched", 0.02, 64),
-    "serving-32": ("batched", "serving", 0.01, 32),
+    "plain-db-scale": ("plain", "plain-db-scale", 1.0, 8,
+                       {"stage_bytes": (1024, 2048, 4096), "max_warps_per_block": (8, 16, 0)}, 3),
+    "batched-512": ("batched", "batched", 0.02, 512, _SMALL_BATCH_GRID, 3),
+    "batched-512-full": ("batched", "batched", 1.0, 512, {"stage_bytes": (1024, 2048), "batch_launch": (1, 2)}, 1),
+    "batched-64": ("batched", "batched", 0.02, 64, _SMALL_BATCH_GRID, 3),
+    "serving-32": ("batched", "serving", 0.01, 32, _SMALL_BATCH_GRID, 3),
+    "serving-4-large": ("batched", "serving", 0.1, 4, {"stage_bytes": (1024, 2048), "batch_launch": (1, 2)}, 3),
 }
-
-GRID = {
-    "stage_bytes": (1024, 2048, 4096),
-    "max_warps_per_block": (8, 16, 0),  # 0: as many as registers allow
-    "tile_residues": (0, 4096, 65536),  # per warp of a block tile; 0: several tiles' worth per warp
-}
+DEFAULT = {"stage_bytes": 1024, "max_warps_per_block": 0, "tile_residues": 0, "batch_launch": 0}
 
 _cache = None
 
@@ -79,11 +88,12 @@ def _time_setting(ps, run, tuning, reps):
     return float(np.median(ms)), out
 
 
-def tune_shape(name: str, reps: int = 3, quick: bool = False) -> dict:
+def tune_shape(name: str, reps: int | None = None, quick: bool = False) -> dict:
     import blaze103
     from blaze103 import synth
 
-    kind, workload, scale, nq = SHAPES[name]
+    kind, workload, scale, nq, grid, shape_reps = SHAPES[name]
+    reps = shape_reps if reps is None else reps
     seed = synth.WORKLOADS[workload]["index"]
     w = synth.make_workload(workload, scale=scale, n_queries=nq, seed=seed)
     rng = np.random.default_rng(seed)
@@ -112,14 +122,13 @@ def tune_shape(name: str, reps: int = 3, quick: bool = False) -> dict:
             run.ms = total
             return outs
 
-    grid = dict(GRID)
-    if kind == "plain":
-        grid["tile_residues"] = (0,)  # single-query runs have no tiles
+    grid = dict(grid)
     if quick:
         grid = {k: v[:2] for k, v in grid.items()}
     rows, ref = [], None
     for vals in itertools.product(*grid.values()):
-        tuning = dict(zip(grid.keys(), vals))
+        tuning = dict(DEFAULT)
+        tuning.update(zip(grid.keys(), vals))
         if kind == "plain":
             ps.set_tuning(**tuning)
             out = run()
@@ -139,9 +148,9 @@ def tune_shape(name: str, reps: int = 3, quick: bool = False) -> dict:
     entry = {"kind": kind, "n_queries": nq, "median_qlen": float(np.median(lengths)),
              "db_residues": int(w.total_residues), "db_subjects": int(w.n_subjects),
              "tuning": rows[0]["tuning"], "ms": rows[0]["ms"],
-             "default_ms": next((r["ms"] for r in rows if r["tuning"] == {
-                 "stage_bytes": 2048, "max_warps_per_block": 0,
-                 "tile_residues": 0}), None),
+             "default_ms": next((r["ms"] for r in rows
+                                 if all(r["tuning"][k] == DEFAULT[k] for k in ("stage_bytes", "max_warps_per_block",
+                                                                                "tile_residues"))), None),
              "grid": rows}
     if kind == "batched":
         batch.close()
@@ -156,7 +165,7 @@ def tune_shape(name: str, reps: int = 3, quick: bool = False) -> dict:
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--shapes", default=",".join(SHAPES))
-    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--reps", type=int, default=None, help="timed repetitions (default: per shape)")
     ap.add_argument("--quick", action="store_true", help="two values per knob")
     ap.add_argument("--out", default=TUNING_PATH)
     args = ap.parse_args()

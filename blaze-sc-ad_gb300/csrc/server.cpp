@@ -25,6 +25,14 @@ constexpr uint64_t kPerQueryFixed = 1u << 20;
 constexpr uint64_t kPerResidue = 512;
 constexpr uint64_t kTableBytes = 4ull * (2 * 21952 + 1 + 686);
 constexpr uint32_t kMaxSlots = 64;  // worker threads (each with its search context)
+// From this many database residues on, a batched run launches the word
+// finder once per query (a query alone fills the GPU) and batching saves
+// nothing on the device: batches are then kept small so that each query's
+// results return soon, and the workers' GPU work runs one batch at a time
+// (their host work -- lookup tables, uploads, results -- still overlaps), since
+// concurrent whole-GPU launches only contend.
+constexpr uint64_t kLargeDbResidues = 1ull << 27;
+constexpr uint32_t kLargeDbBatch = 4;
 
 struct Request {
     uint64_t ticket;
@@ -55,6 +63,9 @@ struct blaze_server {
     uint64_t next_ticket = 1;
     uint64_t in_flight_bytes = 0;
     bool stopping = false;
+    bool one_gpu_batch = false;  // large database: see kLargeDbResidues
+    uint32_t max_batch = 1;      // the configured cap, or kLargeDbBatch on a large database
+    std::mutex gpu_mu;
     std::vector<std::thread> workers;
     // statistics
     uint64_t submitted = 0, completed = 0, batches = 0, residues = 0;
@@ -88,7 +99,7 @@ bool take_batch(blaze_server *s, std::vector<Request> &batch, uint64_t &bytes) {
     }
     const auto deadline = Clock::now() + std::chrono::microseconds(s->cfg.batch_window_us);
     for (;;) {
-        while (!s->queue.empty() && batch.size() < s->cfg.max_batch) {
+        while (!s->queue.empty() && batch.size() < s->max_batch) {
             const uint64_t est = s->queue.front().estimate;
             const uint64_t budget = s->cfg.memory_budget;
             if (!batch.empty() && budget && s->in_flight_bytes + bytes + est > budget) break;
@@ -96,10 +107,10 @@ bool take_batch(blaze_server *s, std::vector<Request> &batch, uint64_t &bytes) {
             batch.push_back(std::move(s->queue.front()));
             s->queue.pop_front();
         }
-        if (batch.size() >= s->cfg.max_batch || s->stopping) break;
+        if (batch.size() >= s->max_batch || s->stopping) break;
         if (s->queue_cv.wait_until(lk, deadline) == std::cv_status::timeout) {
             // take whatever arrived in the last instant
-            while (!s->queue.empty() && batch.size() < s->cfg.max_batch) {
+            while (!s->queue.empty() && batch.size() < s->max_batch) {
                 const uint64_t est = s->queue.front().estimate;
                 if (s->cfg.memory_budget && s->in_flight_bytes + bytes + est > s->cfg.memory_budget) break;
                 bytes += est;
@@ -140,7 +151,11 @@ void worker(blaze_server *s) {
                 batch_residues += s->db_residues;
             }
             if (rc == BLAZE_OK) rc = batch_refill(search, &b, res.data(), off.data(), static_cast<uint32_t>(n), 11);
-            if (rc == BLAZE_OK) rc = blaze_search_run_batch(search, b, params.data(), &n_hsps);
+            if (rc == BLAZE_OK) {
+                std::unique_lock<std::mutex> gpu(s->gpu_mu, std::defer_lock);
+                if (s->one_gpu_batch) gpu.lock();
+                rc = blaze_search_run_batch(search, b, params.data(), &n_hsps);
+            }
             if (rc == BLAZE_OK) {
                 out.resize(n_hsps);
                 rc = blaze_search_batch_results(search, out.data(), n_hsps, &n_hsps);
@@ -196,6 +211,8 @@ extern "C" int blaze_server_create(blaze_db *db, const blaze_server_config *cfg,
     s->cfg = *cfg;
     uint32_t max_len = 0;
     blaze_db_info(db, &s->db_residues, &s->db_subjects, &max_len);
+    s->one_gpu_batch = s->db_residues >= kLargeDbResidues && cfg->tuning.batch_launch != 1;
+    s->max_batch = s->one_gpu_batch ? std::min(cfg->max_batch, kLargeDbBatch) : cfg->max_batch;
     try {
         for (uint32_t i = 0; i < cfg->slots; ++i) s->workers.emplace_back(worker, s);
     } catch (...) {  // a thread that would not start: stop the ones that did

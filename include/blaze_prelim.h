@@ -326,7 +326,12 @@ int blaze_search_set_tuning(blaze_search *s, const blaze_tuning *t);
  * as soon as they are free, admitting queries while the device memory of
  * the in-flight batches (word tables plus a per-query allowance for seed and
  * HSP buffers) stays within memory_budget, so batches overlap on the GPU.
- * Each query's HSP lists are handed back when its batch completes.
+ * Each query's HSP lists are handed back when its batch completes. On a
+ * database of 2^27 residues or more (unless tuning.batch_launch forces
+ * tiles), where a batched run launches the word finder once per query and a
+ * query alone fills the GPU, batches take at most 4 queries and run on the
+ * GPU one at a time (the workers' host work still overlaps): batching saves
+ * nothing there, and concurrent whole-GPU launches only contend.
  */
 typedef struct blaze_server blaze_server;
 
