@@ -381,11 +381,14 @@ def serve_record(local, rank, scale: float, rates, duration: float, max_queries:
     db = blaze103.SeqSrc(w.residues, w.offsets, device=local)
     R = w.total_residues
 
-    def serve(rate, **cfg):
-        srv = blaze103.Server(db, **cfg)
+    def arrivals(rate):
         n = max(20, min(int(rate * duration), max_queries))
-        gaps = rng.exponential(1.0 / rate, n)
-        picks = rng.integers(0, len(pool), n)
+        return rng.exponential(1.0 / rate, n), rng.integers(0, len(pool), n)
+
+    def serve(rate, arr, **cfg):
+        srv = blaze103.Server(db, **cfg)
+        gaps, picks = arr
+        n = len(gaps)
         tickets = []
         due = time.perf_counter()
         for g, k in zip(gaps, picks):
@@ -402,13 +405,14 @@ def serve_record(local, rank, scale: float, rates, duration: float, max_queries:
                 "residues_per_s": st["residues"] / st["busy_s"], "batches": st["batches"],
                 "p50_ms": st["latency_p50_ms"], "p99_ms": st["latency_p99_ms"], "max_ms": st["latency_max_ms"]}
 
-    serve(rates[0], **server_cfg)  # warm-up: contexts, buffers
+    serve(rates[0], arrivals(rates[0]), **server_cfg)  # warm-up: contexts, buffers
     clocks = ClockSampler(local)
     clocks.start()
     sweep = []
     for r in rates:
-        row = {"served": serve(r, **server_cfg)}
-        row["one_at_a_time"] = serve(r, slots=1, max_batch=1, batch_window_us=0)
+        arr = arrivals(r)  # both services see the same queries at the same times
+        row = {"served": serve(r, arr, **server_cfg)}
+        row["one_at_a_time"] = serve(r, arr, slots=1, max_batch=1, batch_window_us=0)
         sweep.append(row)
     clk = clocks.stop()
     db.close()
