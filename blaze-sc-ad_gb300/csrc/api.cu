@@ -239,6 +239,9 @@ extern "C" int blaze_search_free(blaze_search *s) {
     for (auto &kv : s->tile_bounds) kv.second.release();
     s->scratch.release();
     s->init_out.release();
+    s->init_sorted.release();
+    s->dtask.release();
+    s->dres.release();
     s->sorted.release();
     s->work.release();
     s->saved.release();
@@ -337,7 +340,15 @@ struct PassLaunch {
     std::vector<ScanLaunch> scans;
     const GappedArgs *ga;
     bool batched;
+    bool split;  // the gapped stage as prep, lane-parallel DP and finishing kernels
 };
+
+// Batched passes of at least this many queries run the gapped stage with one
+// lane per DP: they hold enough DPs (thousands per SM) for its throughput,
+// while a pass of one or a few queries finishes sooner with a warp per
+// subject (a lane's DP takes too long for a pass that gives each lane one or
+// two of them).
+constexpr uint32_t kGappedSplitMinQueries = 16;
 
 static cudaError_t enqueue_pass(blaze_search *s, const PassLaunch &pl, unsigned event_flags) {
     cudaError_t e = cudaMemsetAsync(s->d_cnt, 0, sizeof(DevCounters), s->stream);
@@ -350,7 +361,9 @@ static cudaError_t enqueue_pass(blaze_search *s, const PassLaunch &pl, unsigned 
                        : launch_scan(l.sa, l.blocks, l.warps_per_block, l.smem_bytes, s->stream);
     }
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(s->ev[2], s->stream, event_flags);
-    if (e == cudaSuccess) e = launch_gapped(*pl.ga, s->gapped_blocks, s->stream);
+    if (e == cudaSuccess)
+        e = pl.split ? launch_gapped_split(*pl.ga, s->gapped_blocks, s->n_sm, s->stream)
+                     : launch_gapped(*pl.ga, s->gapped_blocks, s->stream);
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(s->ev[3], s->stream, event_flags);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s->h_cnt, s->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, s->stream);
@@ -375,7 +388,7 @@ static int launch_pass_graph(blaze_search *s, const PassLaunch &pl) {
         const auto *c = static_cast<const unsigned char *>(p);
         key.insert(key.end(), c, c + n);
     };
-    const int64_t head[2] = {pl.batched, s->gapped_blocks};
+    const int64_t head[3] = {pl.batched, pl.split, s->gapped_blocks};
     put(head, sizeof(head));
     for (const ScanLaunch &l : pl.scans) {
         put(&l.sa, sizeof(ScanArgs));
@@ -484,6 +497,12 @@ static int run_pass(blaze_search *s, const RunSpec &r, const std::vector<ScanPla
     if ((rc = s->work.ensure(work_cap)) != BLAZE_OK) return rc;
     if ((rc = s->out.ensure(s->out_cap)) != BLAZE_OK) return rc;
     const uint32_t nq = batched ? r.b->n : 1u;
+    const bool split = batched && nq >= kGappedSplitMinQueries;
+    if (split) {  // per init-hit slot: ordered init hit, DP task, two DP results
+        if ((rc = s->init_sorted.ensure(s->init_cap)) != BLAZE_OK) return rc;
+        if ((rc = s->dtask.ensure(s->init_cap)) != BLAZE_OK) return rc;
+        if ((rc = s->dres.ensure(2 * s->init_cap)) != BLAZE_OK) return rc;
+    }
     if ((rc = s->groups.ensure(s->out_cap)) != BLAZE_OK) return rc;  // a published list holds >= 1 HSP
     if ((rc = s->qkept.ensure(nq)) != BLAZE_OK) return rc;
     if (batched && (rc = s->work_query.ensure(work_cap)) != BLAZE_OK) return rc;
@@ -495,6 +514,7 @@ static int run_pass(blaze_search *s, const RunSpec &r, const std::vector<ScanPla
 
     PassLaunch pl;
     pl.batched = batched;
+    pl.split = split;
     for (const ScanPlan &plan : plans) {
         const ScanLayout &lay = plan.lay;
         ScanLaunch l;
@@ -586,6 +606,11 @@ static int run_pass(blaze_search *s, const RunSpec &r, const std::vector<ScanPla
     ga.groups = s->groups.p;
     ga.qkept = s->qkept.p;
     ga.cnt = s->d_cnt;
+    if (split) {
+        ga.init_sorted = s->init_sorted.p;
+        ga.dtask = s->dtask.p;
+        ga.dres = s->dres.p;
+    }
     if (batched) {
         ga.work_query = s->work_query.p;
         ga.batch_q = s->bqptr.p;

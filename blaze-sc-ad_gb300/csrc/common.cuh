@@ -42,6 +42,17 @@ struct WorkItem {
     uint64_t first;    // first record in the init-hit array
 };
 
+// One init hit's gapped extension for the lane-parallel DP: the subject, the
+// query (batched: its index) and the gapped start point. Written by the prep
+// kernel at the init hit's slot; valid = 0 for an init hit that is skipped.
+struct DpTask {
+    uint64_t s_base;  // offset of the subject's residues
+    int32_t slen;
+    uint32_t query;
+    int32_t q_off, s_off;
+    int32_t valid, pad;
+};
+
 // A finished gapped HSP as the device writes it (subject = sorted index).
 struct DevHsp {
     uint32_t subject;
@@ -64,6 +75,8 @@ struct DevCounters {
     unsigned int flags;              // kFlag* bits
     unsigned int pad;
     unsigned long long group_count;  // subject HSP lists published (GroupDesc records)
+    unsigned long long next_prep;    // gapped prep-kernel work cursor
+    unsigned long long next_dp;      // lane DP task cursor
 };
 
 // One subject's HSP list in the gapped stage's output, after the preliminary
@@ -161,6 +174,10 @@ struct GappedArgs {
     GroupDesc *groups;       // one per published list (null: none written)
     uint32_t *qkept;         // per query: lists published (null: not counted)
     DevCounters *cnt;
+    // the three-kernel form (launch_gapped_split), per init-hit slot
+    InitHit *init_sorted;    // each item's init hits in processing order
+    DpTask *dtask;
+    int4 *dres;              // per slot: left and right DP (best, row, column, cells; cells -1: not run)
 };
 
 // Hit-list selection: queries that keep more subjects than their
@@ -232,6 +249,10 @@ cudaError_t launch_scan_batch(const ScanArgs &a, int n_blocks, int warps_per_blo
 cudaError_t scan_batch_occupancy(bool query_in_smem, int warps_per_block, size_t smem, int *blocks_per_sm);
 int scan_batch_max_warps_by_registers(bool query_in_smem);
 cudaError_t gapped_occupancy(int *blocks_per_sm);
+// The gapped stage as prep, lane-parallel DP and finishing kernels (batched
+// passes of many queries); n_blocks as for launch_gapped, the DP kernel
+// fills n_sm SMs. Results equal launch_gapped's.
+cudaError_t launch_gapped_split(const GappedArgs &a, int n_blocks, int n_sm, cudaStream_t st);
 
 // Host helpers (host.cpp).
 extern const int32_t kBlosum62[kAlphabet][kAlphabet];

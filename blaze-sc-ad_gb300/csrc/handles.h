@@ -73,6 +73,9 @@ struct blaze_search {
     DevBuf<WorkItem> work;
     DevBuf<DevHsp> saved, out;
     DevBuf<int32_t> dp;
+    DevBuf<InitHit> init_sorted;
+    DevBuf<DpTask> dtask;
+    DevBuf<int4> dres;
     DevCounters *d_cnt = nullptr;
     DevCounters *h_cnt = nullptr;  // pinned
     DevHsp *h_out = nullptr;       // pinned

@@ -14,6 +14,7 @@
 // unlike that filter (whose survivors the CPU re-searches) this kernel
 // produces the final HSPs.
 #include <algorithm>
+#include <mutex>
 #include <cstdint>
 
 #include "common.cuh"
@@ -27,6 +28,12 @@ __device__ const int32_t g_blosum[kAlphabet * kAlphabet] = {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
 
 __device__ __forceinline__ void load_matrix(int32_t *mat) {
     for (int i = threadIdx.x; i < kAlphabet * kAlphabet; i += blockDim.x) mat[i] = g_blosum[i];
@@ -268,6 +275,151 @@ __device__ int purge_and_sort(DevHsp *h, int n) {
     return m;
 }
 
+// One work item of the gapped stage, read and checked.
+struct Item {
+    WorkItem wi;
+    uint32_t qi;
+    const uint8_t *qres, *sub;
+    int32_t qlen, slen, cutoff, smin, max_hsps;
+    uint32_t n;
+    const InitHit *in;
+};
+
+// Reads work item t; false when it must be skipped (a flag is then set).
+__device__ __forceinline__ bool read_item(const GappedArgs &a, unsigned long long t, Item &it, int lane) {
+    it.wi = a.work[t];
+    it.qi = a.work_query ? a.work_query[t] : 0u;
+    const WorkItem &wi = it.wi;
+    if (wi.subject >= a.n_subj || it.qi >= a.n_queries || wi.first > a.init_cap ||
+        wi.n_init > a.init_cap - wi.first) {  // cannot happen: every counted item is written
+        if (lane == 0) atomicOr(&a.cnt->flags, kFlagBadState);
+        return false;
+    }
+    it.qres = a.work_query ? a.batch_q[it.qi] : a.q;
+    it.qlen = a.work_query ? a.batch_qlen[it.qi] : a.qlen;
+    it.cutoff = a.work_query ? a.batch_cutoff[it.qi] : a.cutoff;
+    it.smin = a.work_query ? a.batch_smin[it.qi] : a.smin;
+    it.max_hsps = a.work_query ? a.batch_max_hsps[it.qi] : a.max_hsps;
+    it.n = wi.n_init;
+    it.in = a.init_in + wi.first;
+    const uint64_t o0 = a.off[wi.subject];
+    const uint64_t o1 = a.off[wi.subject + 1];
+    it.sub = a.res + o0;
+    if (it.n > a.cap) {  // cannot happen: the scan kernel only publishes n <= its scratch cap
+        if (lane == 0) atomicOr(&a.cnt->flags, kFlagBadState);
+        return false;
+    }
+    // The DP rows hold dp_stride ints: a subject too long for them (only
+    // possible where the caller sized the rows, as the allocation-free
+    // entry point does) is skipped and reported.
+    if (o1 < o0 || o1 - o0 + 2u > a.dp_stride) {
+        if (lane == 0) atomicOr(&a.cnt->flags, kFlagSubjectTooLong);
+        return false;
+    }
+    it.slen = static_cast<int32_t>(o1 - o0);
+    return true;
+}
+
+// Orders the item's init hits into dst: score descending, ties in discovery
+// order (rank sort; equal records, which only a caller can pass, keep their
+// input order, so every slot is written).
+__device__ __forceinline__ void order_init_hits(const Item &it, InitHit *dst, int lane) {
+    const uint32_t n = it.n;
+    for (uint32_t i = lane; i < n; i += 32) {
+        const InitHit hi = it.in[i];
+        uint32_t rank = 0;
+        for (uint32_t j = 0; j < n; ++j) {
+            const InitHit hj = it.in[j];
+            rank += (init_before(hj, hi) || (j < i && !init_before(hi, hj))) ? 1u : 0u;
+        }
+        dst[rank] = hi;
+    }
+    __syncwarp();
+}
+
+// An init hit must lie inside the query and the subject (the scan kernel's
+// always do; a caller's may not).
+__device__ __forceinline__ bool init_hit_inside(const InitHit &u, const Item &it) {
+    return !(u.len < 1 || u.q_start < 0 || u.s_start < 0 || u.len > it.qlen - u.q_start ||
+             u.len > it.slen - u.s_start);
+}
+
+// Whether init hit u lies inside a kept HSP scoring at least as much.
+__device__ __forceinline__ bool contained(const InitHit &u, const DevHsp *saved, int nsaved, int lane) {
+    bool inside = false;
+    for (int j = lane; j < nsaved; j += 32) {
+        const DevHsp g = saved[j];
+        inside |= u.score <= g.score && g.q_start <= u.q_start && u.q_start + u.len <= g.q_end &&
+                  g.s_start <= u.s_start && u.s_start + u.len <= g.s_end;
+    }
+    return __any_sync(kFull, inside);
+}
+
+__device__ __forceinline__ DevHsp make_hsp(uint32_t subject, int32_t score, int32_t q_off, int32_t s_off,
+                                           int32_t al, int32_t bl, int32_t ar, int32_t br) {
+    DevHsp g;
+    g.subject = subject;
+    g.score = score;
+    g.q_start = q_off + 1 - al;
+    g.q_end = q_off + ar + 1;
+    g.s_start = s_off + 1 - bl;
+    g.s_end = s_off + br + 1;
+    g.q_gs = q_off;
+    g.s_gs = s_off;
+    return g;
+}
+
+// Purges and orders the item's kept HSPs, applies the preliminary E-value
+// reap (E-values fall with the score, so it keeps the leading HSPs scoring
+// at least smin) and max_hsps, and publishes the list.
+__device__ __forceinline__ void publish(const GappedArgs &a, const Item &it, DevHsp *saved, int nsaved, int lane) {
+    int m = 0;
+    if (lane == 0) {
+        const int all = purge_and_sort(saved, nsaved);
+        while (m < all && saved[m].score >= it.smin) ++m;
+        if (it.max_hsps > 0 && m > it.max_hsps) m = it.max_hsps;
+    }
+    m = __shfl_sync(kFull, m, 0);
+    __syncwarp();
+    if (m == 0) return;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&a.cnt->out_count, static_cast<unsigned long long>(m));
+    base = __shfl_sync(kFull, base, 0);
+    if (base + m > a.out_cap) {
+        if (lane == 0) atomicOr(&a.cnt->flags, kFlagOutArrayFull);
+        return;
+    }
+    for (int i = lane; i < m; i += 32) a.out[base + i] = saved[i];
+    if (lane == 0 && a.groups) {
+        // every published list holds at least one of the out_cap HSPs, so
+        // the descriptor index stays below out_cap
+        const unsigned long long gi = atomicAdd(&a.cnt->group_count, 1ull);
+        GroupDesc g;
+        g.first = base;
+        g.query = it.qi;
+        g.subject = it.wi.subject;
+        g.oid = a.oid[it.wi.subject];
+        g.n = static_cast<uint32_t>(m);
+        g.best = saved[0].score;
+        g.pad = 0;
+        a.groups[gi] = g;
+        if (a.qkept) atomicAdd(&a.qkept[it.qi], 1u);
+    }
+}
+
+// Number of work items this pass may take: none when the scan overflowed
+// its init-hit or work array (the host repeats that pass with larger
+// arrays, and an unwritten slot holds no valid item).
+__device__ __forceinline__ unsigned long long work_items(const GappedArgs &a) {
+    unsigned long long n_work = *reinterpret_cast<volatile unsigned long long *>(&a.cnt->work_count);
+    if (n_work > a.work_cap) n_work = a.work_cap;
+    const unsigned scan_flags = *reinterpret_cast<volatile unsigned *>(&a.cnt->flags);
+    if (scan_flags & (kFlagInitArrayFull | kFlagWorkArrayFull | kFlagBadState)) n_work = 0;
+    return n_work;
+}
+
+// The whole gapped stage in one kernel, one warp per work item (single
+// queries, small batches and the allocation-free entry point).
 __global__ void __launch_bounds__(kGappedWarpsPerBlock * 32)
 gapped_kernel(const GappedArgs a) {
     __shared__ int32_t mat[kAlphabet * kAlphabet];
@@ -424,6 +576,357 @@ gapped_kernel(const GappedArgs a) {
 }
 
 // ------------------------------------------------------------------------
+// The gapped stage in three kernels, for batched passes of many queries:
+//
+//   gapped_prep_kernel    one warp per work item: orders its init hits into
+//                         the pass-wide init_sorted array (same slots as the
+//                         scan wrote them) and writes one DP task per init
+//                         hit (its gapped start point);
+//   gapped_dp_kernel      one LANE per X-drop DP (the left and the right one
+//                         of every init hit): each lane runs the sequential
+//                         banded X-drop of the oracle on its own task, rows of
+//                         the warp's 32 tasks in step, its DP row in a
+//                         shared-memory ring of kDpRing columns; a task whose
+//                         band gets wider than the ring is left to the
+//                         finishing kernel;
+//   gapped_finish_kernel  one warp per work item: walks the ordered init
+//                         hits, skips those inside kept HSPs (so the DPs of
+//                         skipped init hits, computed ahead, go unused),
+//                         takes the DP results (running the warp-parallel DP
+//                         for a task the lane kernel left), and publishes.
+//
+// Every DP is independent of the others (containment only decides which
+// results are used), so the results are exactly those of gapped_kernel.
+
+__global__ void __launch_bounds__(kGappedWarpsPerBlock * 32)
+gapped_prep_kernel(const GappedArgs a) {
+    __shared__ int32_t mat[kAlphabet * kAlphabet];
+    load_matrix(mat);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const unsigned long long n_work = work_items(a);
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(&a.cnt->next_prep, 1ull);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= n_work) break;
+        Item it;
+        const bool ok = read_item(a, t, it, lane);
+        const WorkItem wi = a.work[t];
+        if (!ok) {
+            // its tasks stay empty (the checks bounded n_init by init_cap)
+            if (wi.first <= a.init_cap && wi.n_init <= a.init_cap - wi.first)
+                for (uint32_t k = lane; k < wi.n_init; k += 32) a.dtask[wi.first + k].valid = 0;
+            continue;
+        }
+        InitHit *dst = a.init_sorted + wi.first;
+        order_init_hits(it, dst, lane);
+        for (uint32_t k = lane; k < it.n; k += 32) {
+            const InitHit u = dst[k];
+            DpTask d;
+            d.s_base = a.off[wi.subject];
+            d.slen = it.slen;
+            d.query = it.qi;
+            d.q_off = 0;
+            d.s_off = 0;
+            d.valid = init_hit_inside(u, it) ? 1 : 0;
+            d.pad = 0;
+            if (d.valid) {
+                d.q_off = gapped_start(it.qres, it.sub, u.q_start, u.s_start, u.len, mat);
+                d.s_off = d.q_off + (u.s_start - u.q_start);
+            }
+            a.dtask[wi.first + k] = d;
+        }
+    }
+}
+
+// Packed DP cell of the lane kernel's ring: H (21 bits, signed; |H| stays
+// below 2^20, tasks that could score more go to the warp-parallel DP), a
+// dead flag (H is -inf), d = H - gap_extend - E (5 bits: for a cell written
+// live, H - gap_open - gap_extend <= E <= H - gap_extend) and the letter of
+// the NEXT column (5 bits), which the diagonal move into it scores.
+constexpr int kDpRing = 64;            // ring columns per lane (a power of 2)
+constexpr int kDpWarpsPerBlock = 4;
+constexpr int32_t kDpHMax = (1 << 20) - 64;
+constexpr uint32_t kDpDead = 1u << 10;
+
+__device__ __forceinline__ uint32_t dp_pack(int32_t h, int32_t e, int32_t ge, uint32_t letter) {
+    return (static_cast<uint32_t>(h) << 11) | (static_cast<uint32_t>(h - ge - e) << 5) | letter;
+}
+// H = -inf and E = -inf: the H field holds -2^20 and d = 31, so E decodes
+// below every score a band can reach
+__device__ __forceinline__ uint32_t dp_pack_inf(uint32_t letter) {
+    return (static_cast<uint32_t>(-(1 << 20)) << 11) | kDpDead | (31u << 5) | letter;
+}
+
+struct DpConsts {
+    int32_t ge, goe, xdrop, bsize0;
+};
+
+// One lane's task: rows are query letters, columns subject letters, read
+// forwards (right extension) or backwards (left extension) from the start.
+struct DpLane {
+    bool has;
+    unsigned long long t;
+    const uint8_t *S, *Q;  // letter k of the row / column sequence is at [dir * k]
+    int32_t dir, M, N;
+    int32_t row, first, bsize, best, ab, bb, cells, thr, rowoff;
+};
+
+__device__ __forceinline__ void dp_lane_start(DpLane &L, unsigned long long t, const GappedArgs &a,
+                                              const DpConsts &c, uint32_t *R) {
+#define RS(x) R[((x) & (kDpRing - 1)) * 32]
+    L.t = t;
+    L.has = false;
+    const DpTask k = a.dtask[t >> 1];
+    const bool left = (t & 1ull) == 0;
+    const uint8_t *q = a.work_query ? a.batch_q[k.query] : a.q;
+    const int32_t qlen = a.work_query ? a.batch_qlen[k.query] : a.qlen;
+    const uint64_t total = a.off[a.n_subj];
+    // a record is checked before use (every slot is written by the prep
+    // kernel; a stale one from another pass must not send reads astray)
+    if (!k.valid || k.query >= a.n_queries || k.s_base > total || static_cast<uint64_t>(k.slen) > total - k.s_base ||
+        k.q_off < 0 || k.q_off >= qlen || k.s_off < 0 || k.s_off >= k.slen) {
+        if (k.valid) atomicOr(&a.cnt->flags, kFlagBadState);
+        a.dres[t] = make_int4(0, 0, 0, 0);
+        return;
+    }
+    const uint8_t *sb = a.res + k.s_base;
+    int32_t M, N;
+    if (left) {
+        L.dir = -1; L.S = sb + k.s_off + 1; L.Q = q + k.q_off + 1; M = k.q_off + 1; N = k.s_off + 1;
+    } else {
+        L.dir = 1; L.S = sb + k.s_off; L.Q = q + k.q_off; M = qlen - k.q_off - 1; N = k.slen - k.s_off - 1;
+    }
+    L.M = M;
+    L.N = N;
+    if (M <= 0 || N <= 0) {
+        a.dres[t] = make_int4(0, 0, 0, 0);
+        return;
+    }
+    const int32_t bs = N + 1 < c.bsize0 ? N + 1 : c.bsize0;
+    // the packed cell holds H within +-2^20 (BLOSUM62 scores at most 11 per
+    // cell, live cells stay above -xdrop) and d <= 31 (gap_open <= 31)
+    if (bs > kDpRing || 11ll * (M < N ? M : N) >= kDpHMax || c.xdrop >= kDpHMax || c.goe - c.ge > 31) {
+        a.dres[t] = make_int4(0, 0, 0, -1);
+        return;
+    }
+    for (int32_t j = 0; j < bs; ++j) {
+        const int32_t hv = j == 0 ? 0 : -c.goe - (j - 1) * c.ge;
+        const uint32_t letter = j + 1 <= N ? L.S[L.dir * (j + 1)] : 0u;
+        RS(j) = dp_pack(hv, hv - c.goe, c.ge, letter);
+    }
+    L.bsize = bs;
+    L.first = 0;
+    L.row = 1;
+    L.best = L.ab = L.bb = 0;
+    L.cells = bs;
+    L.thr = -c.xdrop;
+    L.rowoff = kAlphabet * static_cast<int32_t>(L.Q[L.dir]);
+    L.has = true;
+}
+
+// The lane's current row: its cells in a tight loop (the sequential band
+// algorithm of the oracle, cell by cell), then the row's end.
+__device__ __forceinline__ void dp_lane_row(DpLane &L, const GappedArgs &a, const DpConsts &c, const int32_t *mat,
+                                            uint32_t *R) {
+    int32_t b = L.first, first = L.first, last = L.first;
+    const int32_t bsize = L.bsize, N = L.N, row = L.row, rowoff = L.rowoff;
+    int32_t h = kNeg, f = kNeg, best = L.best, thr = L.thr, ab = L.ab, bb = L.bb;
+    uint32_t p = RS(b);
+    for (; b < bsize; ++b) {
+        const uint32_t p_n = RS(b + 1);
+        const uint32_t lt = p & 31u;
+        const int32_t hl = static_cast<int32_t>(p) >> 11;
+        const int32_t e = hl - c.ge - static_cast<int32_t>((p >> 5) & 31u);
+        const int32_t hb = (p & kDpDead) ? kNeg : hl;
+        const int32_t sc = mat[rowoff + static_cast<int32_t>(lt)];
+        const int32_t hh = max(max(h, e), f);
+        const bool alive = hh >= thr;
+        const bool up = hh > best;
+        best = up ? hh : best;
+        ab = up ? row : ab;
+        bb = up ? b : bb;
+        thr = up ? hh - c.xdrop : thr;
+        const int32_t eo = hh - c.goe;
+        const int32_t en = max(eo, e - c.ge);
+        f = alive ? max(eo, f - c.ge) : f;
+        last = alive ? b : last;
+        const bool lead = !alive && b == first;
+        first += lead ? 1 : 0;
+        if (!lead) RS(b) = alive ? dp_pack(hh, en, c.ge, lt) : (p | kDpDead);
+        h = b + 1 <= N ? hb + sc : kNeg;
+        p = p_n;
+    }
+    L.best = best;
+    L.thr = thr;
+    L.ab = ab;
+    L.bb = bb;
+    L.first = first;
+    if (first == bsize) {  // no live cell in the row
+        a.dres[L.t] = make_int4(best, ab, bb, L.cells);
+        L.has = false;
+        return;
+    }
+    int32_t bs = bsize;
+    if (last < bs - 1) {
+        // the band ends after its last live cell; that next column's H is
+        // already -inf (a dead cell of this row): make its E -inf too
+        bs = last + 1;
+        if (bs <= N) {
+            RS(bs) = dp_pack_inf(RS(bs) & 31u);
+            bs++;
+        }
+    } else {
+        bool ovf = false;
+        while (f >= thr && bs <= N) {  // the row ended live: extend along its row gap
+            if (bs + 1 - first > kDpRing) { ovf = true; break; }
+            const uint32_t letter = bs + 1 <= N ? L.S[L.dir * (bs + 1)] : 0u;
+            RS(bs) = dp_pack(f, f - c.goe, c.ge, letter);
+            f -= c.ge;
+            bs++;
+        }
+        if (!ovf && bs <= N) {
+            if (bs + 1 - first > kDpRing) {
+                ovf = true;
+            } else {
+                const uint32_t letter = bs + 1 <= N ? L.S[L.dir * (bs + 1)] : 0u;
+                RS(bs) = dp_pack_inf(letter);
+                bs++;
+            }
+        }
+        if (ovf) {  // the band outgrew the ring: the finishing kernel reruns this DP
+            a.dres[L.t] = make_int4(0, 0, 0, -1);
+            L.has = false;
+            return;
+        }
+    }
+    L.bsize = bs;
+    L.row = row + 1;
+    if (L.row > L.M) {
+        a.dres[L.t] = make_int4(best, ab, bb, L.cells);
+        L.has = false;
+        return;
+    }
+    L.rowoff = kAlphabet * static_cast<int32_t>(L.Q[L.dir * L.row]);
+    L.cells += bs - first;
+#undef RS
+}
+
+// Tasks reach a warp in chunks of 32 from a pass-wide cursor (lane 0 takes
+// the next chunk's index ahead); the lanes that need a task take the next
+// ones of the chunk.
+__global__ void __launch_bounds__(kDpWarpsPerBlock * 32)
+gapped_dp_kernel(const GappedArgs a) {
+    __shared__ int32_t mat[kAlphabet * kAlphabet];
+    extern __shared__ __align__(16) uint32_t dp_smem[];
+    load_matrix(mat);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t *R = dp_smem + wib * (kDpRing * 32) + lane;
+    DpConsts c;
+    c.ge = a.gap_extend;
+    c.goe = a.gap_open + a.gap_extend;
+    c.xdrop = a.xdrop < c.goe ? c.goe : a.xdrop;
+    c.bsize0 = 1 + (c.xdrop - c.goe) / c.ge + 1;
+    unsigned long long n_init = 0;
+    {
+        n_init = *reinterpret_cast<volatile unsigned long long *>(&a.cnt->init_count);
+        if (n_init > a.init_cap) n_init = a.init_cap;
+        if (work_items(a) == 0) n_init = 0;
+    }
+    const unsigned long long n = 2ull * n_init;
+    unsigned long long next = 0, cur;
+    if (lane == 0) next = atomicAdd(&a.cnt->next_dp, 32ull);
+    cur = __shfl_sync(kFull, next, 0);
+    int32_t cnt = cur < n ? static_cast<int32_t>(n - cur < 32ull ? n - cur : 32ull) : 0, qpos = 0;
+    if (lane == 0) next = atomicAdd(&a.cnt->next_dp, 32ull);
+    DpLane L;
+    L.has = false;
+    for (;;) {
+        unsigned need = __ballot_sync(kFull, !L.has);
+        while (need) {
+            if (qpos >= cnt) {  // the next chunk
+                cur = __shfl_sync(kFull, next, 0);
+                cnt = cur < n ? static_cast<int32_t>(n - cur < 32ull ? n - cur : 32ull) : 0;
+                qpos = 0;
+                if (lane == 0 && cur < n) next = atomicAdd(&a.cnt->next_dp, 32ull);
+            }
+            const int32_t idx = qpos + __popc(need & lanemask_lt());
+            qpos += __popc(need);
+            if (!L.has && idx < cnt) dp_lane_start(L, cur + idx, a, c, R);
+            if (cnt == 0) break;  // no task left for anyone
+            need = __ballot_sync(kFull, !L.has);
+        }
+        if (__ballot_sync(kFull, L.has) == 0) break;
+        if (L.has) dp_lane_row(L, a, c, mat, R);
+    }
+}
+
+__global__ void __launch_bounds__(kGappedWarpsPerBlock * 32)
+gapped_finish_kernel(const GappedArgs a) {
+    __shared__ int32_t mat[kAlphabet * kAlphabet];
+    load_matrix(mat);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const unsigned long long gwarp = (static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    DevHsp *saved = a.saved + gwarp * a.cap;
+    int32_t *Hb = a.dp + gwarp * 2ull * a.dp_stride;
+    int32_t *Eb = Hb + a.dp_stride;
+    const unsigned long long n_work = work_items(a);
+    unsigned long long cells = 0, n_ext = 0;
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(&a.cnt->next_gapped, 1ull);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= n_work) break;
+        Item it;
+        if (!read_item(a, t, it, lane)) continue;  // flagged by the prep kernel already
+        const InitHit *sorted = a.init_sorted + it.wi.first;
+        const DpTask *tasks = a.dtask + it.wi.first;
+        const int4 *res = a.dres + 2ull * it.wi.first;
+        int nsaved = 0;
+        for (uint32_t k = 0; k < it.n; ++k) {
+            const InitHit u = sorted[k];
+            if (!init_hit_inside(u, it)) {
+                if (lane == 0) atomicOr(&a.cnt->flags, kFlagBadInitHit);
+                continue;
+            }
+            if (contained(u, saved, nsaved, lane)) continue;
+            const int32_t q_off = tasks[k].q_off;
+            const int32_t s_off = q_off + (u.s_start - u.q_start);
+            const int4 rl = res[2 * k], rr = res[2 * k + 1];
+            int32_t left = rl.x, al = rl.y, bl = rl.z, right = rr.x, ar = rr.y, br = rr.z;
+            if (rl.w < 0) {
+                left = xdrop_dp<true>(it.qres, it.sub, q_off + 1, s_off + 1, a.gap_open, a.gap_extend, a.xdrop, mat, Hb,
+                                      Eb, &al, &bl, &cells);
+            } else {
+                cells += static_cast<unsigned long long>(rl.w);
+            }
+            if (rr.w < 0) {
+                ar = br = 0;
+                right = xdrop_dp<false>(it.qres + q_off, it.sub + s_off, it.qlen - q_off - 1, it.slen - s_off - 1,
+                                        a.gap_open, a.gap_extend, a.xdrop, mat, Hb, Eb, &ar, &br, &cells);
+            } else {
+                cells += static_cast<unsigned long long>(rr.w);
+            }
+            ++n_ext;
+            const int32_t score = left + right;
+            if (score >= it.cutoff) {
+                if (lane == 0) saved[nsaved] = make_hsp(it.wi.subject, score, q_off, s_off, al, bl, ar, br);
+                ++nsaved;
+            }
+            __syncwarp();
+        }
+        publish(a, it, saved, nsaved, lane);
+    }
+    if (lane == 0) {
+        atomicAdd(&a.cnt->dp_cells, cells);
+        atomicAdd(&a.cnt->gapped_ext, n_ext);
+    }
+}
+
+// ------------------------------------------------------------------------
 // Hit-list selection (hitlist_size, max_target_seqs), for the queries whose
 // kept subjects outnumber their limit. The ranking key orders subjects by
 // the score of their best HSP, then by smaller OID; keys within a query are
@@ -498,6 +1001,33 @@ cudaError_t launch_hitlist(const HitlistArgs &a, uint32_t n_select, int n_sm, cu
 cudaError_t launch_gapped(const GappedArgs &a, int n_blocks, cudaStream_t st, int warps_per_block) {
     if (warps_per_block < 1 || warps_per_block > kGappedWarpsPerBlock) return cudaErrorInvalidValue;
     gapped_kernel<<<n_blocks, warps_per_block * 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gapped_split(const GappedArgs &a, int n_blocks, int n_sm, cudaStream_t st) {
+    constexpr size_t ring_bytes = sizeof(uint32_t) * kDpWarpsPerBlock * kDpRing * 32;
+    // per device: the DP kernel's occupancy
+    constexpr int kMaxDevices = 64;
+    static std::once_flag once[kMaxDevices];
+    static cudaError_t setup_of[kMaxDevices];
+    static int per_sm_of[kMaxDevices];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::call_once(once[dev], [dev] {
+        per_sm_of[dev] = 1;
+        setup_of[dev] = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_of[dev], gapped_dp_kernel,
+                                                                      kDpWarpsPerBlock * 32, ring_bytes);
+    });
+    if (setup_of[dev] != cudaSuccess) return setup_of[dev];
+    gapped_prep_kernel<<<n_blocks, kGappedWarpsPerBlock * 32, 0, st>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    gapped_dp_kernel<<<n_sm * std::max(per_sm_of[dev], 1), kDpWarpsPerBlock * 32, ring_bytes, st>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    gapped_finish_kernel<<<n_blocks, kGappedWarpsPerBlock * 32, 0, st>>>(a);
     return cudaGetLastError();
 }
 

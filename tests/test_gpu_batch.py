@@ -39,12 +39,12 @@ def _plain(ps, db, q, p):
         qq.close()
 
 
-def _check_batch_equals_plain(tuning=None):
-    qs = _queries()
+def _check_batch_equals_plain(tuning=None, qs=None, **override):
+    qs = qs or _queries()
     res, off = _db(with_homologs_of=qs)
     db = blaze103.SeqSrc(res, off)
     ps = blaze103.PrelimSearch(db)
-    params = [params_for(len(q), db.tot_len, db.num_seqs)[0] for q in qs]
+    params = [params_for(len(q), db.tot_len, db.num_seqs, **override)[0] for q in qs]
     want = [_plain(ps, db, q, p) for q, p in zip(qs, params)]
     if tuning:
         ps.set_tuning(**tuning)
@@ -91,6 +91,36 @@ def test_batch_capacity_regrowth(monkeypatch):
     monkeypatch.setenv("BLAZE_INITIAL_OUT_CAP", "5")
     monkeypatch.setenv("BLAZE_INITIAL_WORK_CAP", "3")
     _check_batch_equals_plain()
+
+
+# Batches of at least 16 queries run the gapped stage with one lane per DP
+# (prep, DP and finishing kernels); these batches must give the plain path's
+# lists too, including DPs whose band outgrows the lane's 64-column ring or
+# whose gap costs the packed ring cells cannot hold (rerun warp-parallel).
+def _queries20(seed=23):
+    rng = np.random.default_rng(seed)
+    lengths = (5, 50, 120, 300, 333, 700, 1000, 1500, 2600, 9000,
+               64, 90, 150, 210, 260, 410, 520, 640, 880, 1200)
+    return [synth.random_residues(rng, L) for L in lengths]
+
+
+@pytest.mark.parametrize("tuning", [None, dict(launch_mode=1), dict(launch_mode=2, batch_launch=1),
+                                    dict(batch_launch=2)])
+def test_lane_dp_batch_equals_plain(tuning):
+    _check_batch_equals_plain(tuning, qs=_queries20())
+
+
+def test_lane_dp_capacity_regrowth(monkeypatch):
+    monkeypatch.setenv("BLAZE_INITIAL_SCRATCH_CAP", "2")
+    monkeypatch.setenv("BLAZE_INITIAL_INIT_CAP", "5")
+    monkeypatch.setenv("BLAZE_INITIAL_OUT_CAP", "5")
+    monkeypatch.setenv("BLAZE_INITIAL_WORK_CAP", "3")
+    _check_batch_equals_plain(qs=_queries20())
+
+
+@pytest.mark.parametrize("override", [dict(gapped_xdrop=100), dict(gap_open=40), dict(gap_open=0, gap_extend=2)])
+def test_lane_dp_fallbacks_and_gap_costs(override):
+    _check_batch_equals_plain(qs=_queries20(), **override)
 
 
 def test_batch_rejects_mixed_search_settings():
