@@ -3,7 +3,8 @@ single-subject and long subjects, rare residue codes, low-complexity runs,
 planted homologs, unsorted OIDs), queries of 1 to 12,000 residues, varied
 search parameters and launch shapes. Each case checks the plain search
 against the oracle (init hits and HSPs), and some also the traceback against
-the oracle's and a batched run against the plain runs of its queries."""
+the oracle's and a batched run (a few queries, or 16 and more) against the
+plain runs of its queries."""
 import numpy as np
 import pytest
 
@@ -110,7 +111,10 @@ def run_case(seed):
             for f in TB_FIELDS:
                 assert tb[f].tolist() == [r[f] for r in tref], f"seed {seed}: traceback field {f}"
         if rng.random() < 0.35:
-            qs = [q] + [synth.random_residues(rng, int(rng.integers(1, 1500))) for _ in range(int(rng.integers(1, 6)))]
+            # a few queries (one warp per subject in the gapped stage) or 16
+            # and more (one lane per DP)
+            n_more = int(rng.integers(1, 6)) if rng.random() < 0.5 else int(rng.integers(15, 24))
+            qs = [q] + [synth.random_residues(rng, int(rng.integers(1, 1500))) for _ in range(n_more)]
             plist, plain = [], []
             for qq in qs:
                 p, _ = params_for(len(qq), max(int(off[-1]), 1), max(len(seqs), 1), **override)
