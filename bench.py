@@ -279,19 +279,32 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def batched_record(local, rank, world, scale: float, n_queries: int, warmup: int, passes: int,
-                   check_subjects: int = 5000) -> dict:
-    """Batched form vs the plain path on the same queries and database
-    (batched workload: 512 queries, lengths log-normal, median 350, clipped
-    50-2,000; 5M subjects at scale 1; 10% planted homologs), both timed with
-    CUDA events on the search stream. Also checked: the batched HSPs equal the
-    plain path's for every query, and both equal the oracle's on every k-th
-    subject (about check_subjects of them, whole-database statistics)."""
+# The batched records' workloads: name, seed and description.
+BATCHED_WORKLOADS = {
+    "batched": (2, "batched", "log-normal median 350, 50-2000 aa", "10% planted homologs"),
+    "overflow-stress": (3, "extension and overflow stress", "2000-5000 aa",
+                        "lengths log-normal (median 250) with the longest 0.1% at 15000-35000 aa, 20% with "
+                        "low-complexity runs, 25% planted homologs at 30-60% identity"),
+}
+
+
+def batched_record(local, rank, world, scale: float, n_queries, warmup: int, passes: int,
+                   check_subjects: int = 5000, workload: str = "batched") -> dict:
+    """Batched form vs the plain path on the same queries and database, both
+    timed with CUDA events on the search stream: the batched workload (512
+    queries, lengths log-normal, median 350, clipped 50-2,000; 5M subjects at
+    scale 1; 10% planted homologs) or the extension and overflow stress (64
+    queries of 2,000-5,000 residues; 500,000 subjects up to 35,000 residues,
+    low-complexity runs, 25% homologs at 30-60% identity). Also checked: the
+    batched HSPs equal the plain path's for every query, and both equal the
+    oracle's on every k-th subject (about check_subjects of them,
+    whole-database statistics)."""
     import blaze103
     import oracle
     from blaze103 import synth
 
-    w = synth.make_workload("batched", scale=scale, n_queries=n_queries, seed=2 + 7919 * rank)
+    seed0, label, qdesc, ddesc = BATCHED_WORKLOADS[workload]
+    w = synth.make_workload(workload, scale=scale, n_queries=n_queries, seed=seed0 + 7919 * rank)
     db_total, db_n = w.total_residues * world, w.n_subjects * world
     db = blaze103.SeqSrc(w.residues, w.offsets, device=local)
     ps = blaze103.PrelimSearch(db)
@@ -343,9 +356,11 @@ def batched_record(local, rank, world, scale: float, n_queries: int, warmup: int
         "metric": "DB residues/s per query, batched form (aggregate over queries)",
         "value": nq * R / b_s, "unit": UNIT, "passes": passes, "warmup": warmup,
         "ms_per_pass": b_s * 1e3,
-        "config": {"workload": f"batched: {nq} queries (log-normal median 350, 50-2000 aa) vs "
-                               f"{w.n_subjects} subjects / {R} residues, 10% planted homologs",
-                   "db_subjects": w.n_subjects, "db_residues": R, "queries": nq, "database_scale": scale},
+        "config": {"workload": f"{label}: {nq} queries ({qdesc}) vs "
+                               f"{w.n_subjects} subjects / {R} residues, {ddesc}",
+                   "db_subjects": w.n_subjects, "db_residues": R, "queries": nq, "database_scale": scale,
+                   "longest_subject": int(np.diff(w.offsets.astype(np.int64)).max()),
+                   "query_lengths": [min(len(q) for q in w.queries), max(len(q) for q in w.queries)]},
         "plain_same_workload": {"value": nq * R / p_s, "ms_per_pass": p_s * 1e3,
                                 "form": "one search per query (scan + gapped launch sequence each)"},
         "batched_over_plain": p_s / b_s,
@@ -470,6 +485,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="plain line without its batched sub-record")
     ap.add_argument("--no-serve", action="store_true", help="plain line without its serving sub-record")
+    ap.add_argument("--no-stress", action="store_true", help="plain line without its overflow-stress sub-record")
+    ap.add_argument("--stress-scale", type=float, default=1.0,
+                    help="overflow-stress sub-record: database size relative to 500,000 subjects")
     ap.add_argument("--batched-scale", type=float, default=1.0,
                     help="batched sub-record: database size relative to 5M subjects")
     ap.add_argument("--serve-scale", type=float, default=0.1,
@@ -668,6 +686,9 @@ def main():
     # sub-records (N=1 only): the batched form and the serving loop
     if world == 1 and not args.no_batched:
         line["batched"] = batched_record(local, rank, world, args.batched_scale, args.queries, 1, 1)
+    if world == 1 and not args.no_stress:
+        line["stress"] = batched_record(local, rank, world, args.stress_scale, None, 1, 1,
+                                        workload="overflow-stress")
     if world == 1 and not args.no_serve:
         rates = [float(x) for x in args.serve_rates.split(",")]
         line["serve"] = serve_record(local, rank, args.serve_scale, rates, args.duration, args.max_queries,

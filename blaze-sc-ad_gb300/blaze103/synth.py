@@ -5,7 +5,9 @@ arrays plus offsets).
 
 Residues are NCBIstdaa codes of the 20 standard amino acids drawn i.i.d. from
 the Robinson-Robinson background frequencies. Subject lengths are log-normal
-(median 250, sigma 0.82 so the mean is ~350), clipped, sorted ascending.
+(median 250, sigma 0.82 so the mean is ~350), clipped, sorted ascending; the
+overflow-stress workload's longest 0.1% are drawn uniformly up to its clip
+(35,000), which the log-normal alone would not reach.
 Planted homologs copy a 100-300 residue window of a query, substitute
 residues toward a target identity using BLOSUM62 target frequencies
 (q_ab ~ p_a p_b exp(lambda s_ab)), and insert/delete at 2% per residue with
@@ -124,7 +126,8 @@ WORKLOADS = {
     "batched": dict(index=2, query_lengths=("lognormal", 512, 350, 50, 2000), n_subjects=5_000_000,
                     clip=(30, 5000), homolog_frac=0.10, identity=(0.40, 0.40), lowcomplex_frac=0.0),
     "overflow-stress": dict(index=3, query_lengths=("uniform", 64, 2000, 5000), n_subjects=500_000,
-                            clip=(30, 35000), homolog_frac=0.25, identity=(0.30, 0.60), lowcomplex_frac=0.20),
+                            clip=(30, 35000), homolog_frac=0.25, identity=(0.30, 0.60), lowcomplex_frac=0.20,
+                            long_tail=(0.001, 15_000, 35_000)),
     "serving": dict(index=4, query_lengths=("lognormal", 256, 350, 30, 5000), n_subjects=10_000_000,
                     clip=(30, 5000), homolog_frac=0.01, identity=(0.40, 0.40), lowcomplex_frac=0.0),
 }
@@ -155,6 +158,11 @@ def make_workload(workload, scale: float = 1.0, seed: int | None = None,
     n = max(int(round(c["n_subjects"] * scale)), 1)
     lo, hi = c["clip"]
     lengths = np.sort(lognormal_lengths(rng, n, median, sigma, lo, hi))
+    if c.get("long_tail"):  # the longest subjects reach the clip: lengths uniform in [a, b]
+        frac, a, b = c["long_tail"]
+        n_long = int(round(frac * n))
+        if n_long:
+            lengths[n - n_long:] = np.sort(rng.integers(a, b + 1, size=n_long))
     offsets = np.zeros(n + 1, dtype=np.uint64)
     np.cumsum(lengths, out=offsets[1:])
     residues = random_residues(rng, int(offsets[-1]))
