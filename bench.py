@@ -259,7 +259,9 @@ def run_reference(args, rank, world):
                                                     w.total_residues * world, w.n_subjects * world)
         t_all += dt
         n_all += n_res
-        sample = (f"8 queries x every {int(round(1 / frac))}th subject of the "
+        k = max(int(round(1 / frac)), 1)
+        which = "all subjects" if k == 1 else f"every {k}th subject"
+        sample = (f"8 queries x {which} of the "
                   f"{w.n_subjects}-subject database ({n_subj} subjects, "
                   f"{n_res // 8} residues) per step, the cpu_baseline sample")
     value = n_all / t_all
@@ -479,7 +481,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="blaze", choices=["blaze", "reference"])
     ap.add_argument("--scale", type=float, default=1.0, help="database size relative to the default workload (2M subjects)")
-    ap.add_argument("--cpu-frac", type=float, default=0.25, help="cpu_baseline sample fraction")
+    ap.add_argument("--cpu-frac", type=float, default=1.0,
+                    help="cpu_baseline (and parity) sample: this fraction of the subjects (1: all)")
     ap.add_argument("--ref-frac", type=float, default=None,
                     help="reference arm sample fraction per step (default: the cpu_baseline fraction)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -668,15 +671,16 @@ def main():
         rate, dt, n_res, n_subj, sample = cpu_sample_run(w, w.queries, args.cpu_frac, threads, db_total, db_n,
                                                          keep=True)
         k = max(int(round(1.0 / args.cpu_frac)), 1)
+        which = "all subjects" if k == 1 else f"every {k}th subject"
         line["cpu_baseline"] = {
             "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"8 queries x every {k}th subject "
+            "sample": f"8 queries x {which} "
                       f"({n_subj} subjects, {n_res // 8} residues), {dt:.1f} s",
         }
         # the oracle's HSPs of that sample against the e2e path's, same OIDs
         par = parity_check(sample[0], sample[1], e2e_out, k)
         par.update({"subjects_checked": n_subj, "queries": len(w.queries),
-                    "sample": f"every {k}th subject, whole-database statistics",
+                    "sample": f"{which}, whole-database statistics",
                     "path": "e2e (blaze_prelim_search)", "oracle": "oracle/blaze_oracle.c"})
         line["parity"] = par
     for q in queries:

@@ -114,4 +114,4 @@ def test_both_arms_report_the_same_config():
     bench = _bench_module()
     w = synth.make_workload("plain-db-scale", scale=0.001, seed=1)
     assert line["config"] == bench.plain_config(w, 1)
-    assert "every 4th subject" in line["cpu_baseline"]["sample"]
+    assert "all subjects" in line["cpu_baseline"]["sample"]  # the cpu_baseline sample: the whole database
