@@ -496,6 +496,10 @@ def main():
     ap.add_argument("--serve-scale", type=float, default=0.1,
                     help="serving sub-record: database size relative to 10M subjects")
     ap.add_argument("--serve-rates", default="20,100,400", help="serving sub-record: arrival rates, queries/s")
+    ap.add_argument("--serve-small-scale", type=float, default=0.01,
+                    help="second serving sub-record (serve_small): a database where one query leaves the GPU "
+                         "mostly idle (0: none)")
+    ap.add_argument("--serve-small-rates", default="100,2000", help="serve_small: arrival rates, queries/s")
     ap.add_argument("--mode", default="plain", choices=["plain", "batched", "serve"],
                     help="plain: the drop-in, one query per launch sequence (the headline line); "
                          "batched: many queries per launch against a 5M-subject-shaped database, scaled")
@@ -697,6 +701,10 @@ def main():
         rates = [float(x) for x in args.serve_rates.split(",")]
         line["serve"] = serve_record(local, rank, args.serve_scale, rates, args.duration, args.max_queries,
                                      server_config(args))
+        if args.serve_small_scale > 0:
+            rates = [float(x) for x in args.serve_small_rates.split(",")]
+            line["serve_small"] = serve_record(local, rank, args.serve_small_scale, rates, args.duration,
+                                               args.max_queries, server_config(args))
     if rank == 0:
         print(json.dumps(line), flush=True)
     group.close()
